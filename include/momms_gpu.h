@@ -1,0 +1,124 @@
+/*
+ * momms_gpu.h - C ABI of the GB300 (sm_103a) blocked matrix multiply.
+ *
+ * One call computes C := beta*C + alpha*A*B for an m x k matrix A, a k x n
+ * matrix B and an m x n matrix C, each given as a strided view: element (i, j)
+ * of an operand lives at ptr[i*rs + j*cs] (counted in elements). Column-major
+ * storage is rs = 1, cs = leading dimension; row-major is cs = 1.
+ *
+ * It replaces, as one node, the reference's composed subtree
+ *     PartN -> PartK -> PackB -> PartM -> PackA -> ParallelN -> KernelNM -> microkernel
+ * (src/exper/l3_packing.rs:58-66 of tlrmchlsmth/momms), whose only foreign
+ * function boundary is the BLIS microkernel
+ *     bli_dgemm_haswell_asm_6x8(k, *alpha, *a, *b, *beta, *c, rs_c, cs_c, *aux, *cntx)
+ *     (ukernels/bli_gemm_haswell_asm_d6x8.c:666-676, bound in Rust at
+ *      src/kern/ukernel_wrapper.rs:40-53 and :73-90).
+ * The operand contract follows the reference's views: alpha is the product of
+ * the A and B scalars and beta is the C scalar (src/kern/kernel_nm.rs:44-45);
+ * a view's pointer is the buffer at the view offset (RoCM::get_buffer,
+ * src/matrix/general_stride.rs:244-257) with the matrix's row and column
+ * strides (:42-43).
+ *
+ * Errors are returned as momms_status codes (the reference panics instead,
+ * e.g. src/kern/ukernel_wrapper.rs:23-28); momms_last_error() gives a message.
+ * No entry point throws or aborts.
+ *
+ * Memory: an operand flagged MOMMS_MEM_HOST (or detected as host memory under
+ * MOMMS_MEM_AUTO) is staged through device memory by the library and the call
+ * returns after C has been copied back. When all operands are device memory
+ * the call is asynchronous on `stream` (a cudaStream_t; NULL = legacy default
+ * stream).
+ */
+#ifndef MOMMS_GPU_H
+#define MOMMS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MOMMS_ABI_VERSION 1
+
+typedef enum {
+  MOMMS_OK = 0,
+  MOMMS_ERR_INVALID_ARG = 1,    /* negative size, null pointer, bad enum */
+  MOMMS_ERR_UNSUPPORTED = 2,    /* dtype / precision combination not provided */
+  MOMMS_ERR_CUDA = 3,           /* a CUDA runtime call failed */
+  MOMMS_ERR_NO_DEVICE = 4,      /* no usable CUDA device */
+  MOMMS_ERR_OUT_OF_MEMORY = 5,  /* device allocation failed */
+  MOMMS_ERR_DEVICE_TIMEOUT = 6, /* a kernel's bounded wait expired */
+  MOMMS_ERR_ADMISSION = 7,      /* serving: request larger than the budget */
+  MOMMS_ERR_BUSY = 8,           /* serving: queue full or not ready */
+  MOMMS_ERR_SHUTDOWN = 9        /* serving: server stopped */
+} momms_status;
+
+typedef enum { MOMMS_DTYPE_F64 = 0, MOMMS_DTYPE_F32 = 1 } momms_dtype;
+
+/* How the products are formed.
+ * PLAIN: f64 on FP64 tensor-core MMA (DMMA); f32 on register-blocked FFMA.
+ * The other modes are added by later entries of this header. */
+typedef enum {
+  MOMMS_PREC_PLAIN = 0,
+  MOMMS_PREC_OZAKI = 1,      /* f64 only: FP64 emulated from fp16 slices on tcgen05 */
+  MOMMS_PREC_SPLIT_TF32 = 2  /* f32 only: 3-term split TF32 on tcgen05 */
+} momms_precision;
+
+typedef enum { MOMMS_MEM_AUTO = 0, MOMMS_MEM_HOST = 1, MOMMS_MEM_DEVICE = 2 } momms_memspace;
+
+/* A strided matrix view: element (i, j) at ptr[i*rs + j*cs]. */
+typedef struct {
+  void* ptr;
+  int64_t rs;
+  int64_t cs;
+  int32_t mem; /* momms_memspace */
+  int32_t reserved;
+} momms_operand;
+
+/* One GEMM request: C := beta*C + alpha*A*B. */
+typedef struct {
+  int32_t dtype;     /* momms_dtype */
+  int32_t precision; /* momms_precision */
+  int64_t m, n, k;
+  double alpha, beta; /* used in the operands' dtype */
+  momms_operand a, b, c;
+  double target_rel_err; /* OZAKI: requested max |dC_ij| / (|A||B|)_ij; 0 = FP64 level */
+  int32_t slices;        /* OZAKI: slice count, 0 = chosen from target_rel_err */
+  int32_t flags;         /* reserved, must be 0 */
+} momms_gemm_desc;
+
+/* The node entry point: the GPU replacement of the composed subtree above. */
+int momms_gemm(const momms_gemm_desc* desc, void* stream);
+
+/* Typed convenience forms with the argument meaning of the reference
+ * microkernel (alpha and beta passed by pointer, C strides rs_c / cs_c),
+ * extended by m, n and the A / B strides because the node also replaces the
+ * packing layers. Memory space is detected per operand (MOMMS_MEM_AUTO). */
+int momms_dgemm(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c, int64_t rs_c,
+                int64_t cs_c, void* stream);
+int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float* a, int64_t rs_a, int64_t cs_a,
+                const float* b, int64_t rs_b, int64_t cs_b, const float* beta, float* c, int64_t rs_c,
+                int64_t cs_c, void* stream);
+
+/* Checks a descriptor without touching the GPU: sizes, strides, enums.
+ * Returns MOMMS_OK or MOMMS_ERR_INVALID_ARG / MOMMS_ERR_UNSUPPORTED. */
+int momms_gemm_validate(const momms_gemm_desc* desc);
+
+/* Reads and clears the current device's status word (bits set by kernels
+ * whose bounded waits expired). Returns MOMMS_OK or MOMMS_ERR_DEVICE_TIMEOUT;
+ * *bits (if non-null) receives the raw word. Synchronises the device. */
+int momms_device_status(uint32_t* bits);
+
+/* Static description of the error codes, and the last error message of the
+ * calling thread (empty string if none). */
+const char* momms_status_string(int status);
+const char* momms_last_error(void);
+
+/* ABI version of the loaded library (MOMMS_ABI_VERSION at build time). */
+int momms_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOMMS_GPU_H */

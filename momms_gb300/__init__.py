@@ -1,0 +1,99 @@
+"""momms_gb300: the GB300 (sm_103a) blocked matrix multiply C := beta*C + alpha*A*B.
+
+The product is the shared library ``libmomms_gpu.so`` built from ``csrc/``;
+its C ABI is ``include/momms_gpu.h``. This package loads that library and
+gives Python callers the same view-based interface the reference exposes
+(``momms_gb300.matrix.Matrix`` and the ``GemmNode`` family in
+``momms_gb300.nodes``). There is no CPU fallback: if the library is missing,
+loading it raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmomms_gpu.so")
+
+# momms_status
+OK = 0
+ERR_INVALID_ARG = 1
+ERR_UNSUPPORTED = 2
+ERR_CUDA = 3
+ERR_NO_DEVICE = 4
+ERR_OUT_OF_MEMORY = 5
+ERR_DEVICE_TIMEOUT = 6
+ERR_ADMISSION = 7
+ERR_BUSY = 8
+ERR_SHUTDOWN = 9
+
+DTYPE_F64 = 0
+DTYPE_F32 = 1
+PREC_PLAIN = 0
+PREC_OZAKI = 1
+PREC_SPLIT_TF32 = 2
+MEM_AUTO = 0
+MEM_HOST = 1
+MEM_DEVICE = 2
+
+
+class Operand(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("rs", ctypes.c_int64), ("cs", ctypes.c_int64),
+                ("mem", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class GemmDesc(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("m", ctypes.c_int64), ("n", ctypes.c_int64), ("k", ctypes.c_int64),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("a", Operand), ("b", Operand), ("c", Operand),
+                ("target_rel_err", ctypes.c_double), ("slices", ctypes.c_int32),
+                ("flags", ctypes.c_int32)]
+
+
+class MommsError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"momms status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load (once) and return the ctypes handle of libmomms_gpu.so."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: build it with `python -m momms_gb300.build` "
+                          "(or __graft_entry__.build()); there is no CPU fallback")
+    lib = ctypes.CDLL(p)
+    vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.momms_gemm.argtypes = [ctypes.POINTER(GemmDesc), vp]
+    lib.momms_gemm.restype = i32
+    lib.momms_gemm_validate.argtypes = [ctypes.POINTER(GemmDesc)]
+    lib.momms_gemm_validate.restype = i32
+    for name, ct in (("momms_dgemm", ctypes.c_double), ("momms_sgemm", ctypes.c_float)):
+        f = getattr(lib, name)
+        P = ctypes.POINTER(ct)
+        f.argtypes = [i64, i64, i64, P, vp, i64, i64, vp, i64, i64, P, vp, i64, i64, vp]
+        f.restype = i32
+    lib.momms_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    lib.momms_device_status.restype = i32
+    lib.momms_status_string.argtypes = [i32]
+    lib.momms_status_string.restype = ctypes.c_char_p
+    lib.momms_last_error.argtypes = []
+    lib.momms_last_error.restype = ctypes.c_char_p
+    lib.momms_abi_version.argtypes = []
+    lib.momms_abi_version.restype = i32
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status, lib=None):
+    """Raise MommsError for a non-zero status."""
+    if status != OK:
+        lib = lib or load_library()
+        raise MommsError(status, lib.momms_last_error().decode() or lib.momms_status_string(status).decode())
+    return status

@@ -1,0 +1,384 @@
+// The C ABI of include/momms_gpu.h: argument checks, memory-space detection,
+// host<->device staging, dispatch to the kernels, error reporting.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace momms {
+
+namespace {
+thread_local char g_last_error[512] = "";
+std::mutex g_dev_mu;
+DeviceState g_devices[64];
+}  // namespace
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky-free error so the next call starts clean
+  if (e == cudaErrorMemoryAllocation) return fail(MOMMS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return fail(MOMMS_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return fail(MOMMS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+DeviceState* device_state() {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    cuda_fail(e == cudaSuccess ? cudaErrorInvalidDevice : e, "cudaGetDevice");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  DeviceState& d = g_devices[dev];
+  if (d.device < 0) {
+    int sms = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+      cuda_fail(e, "cudaDeviceGetAttribute");
+      return nullptr;
+    }
+    unsigned* st = nullptr;
+    if ((e = cudaMalloc(&st, sizeof(unsigned))) != cudaSuccess) {
+      cuda_fail(e, "status word");
+      return nullptr;
+    }
+    if ((e = cudaMemset(st, 0, sizeof(unsigned))) != cudaSuccess) {
+      cuda_fail(e, "status word");
+      return nullptr;
+    }
+    d.sm_count = sms;
+    d.status = st;
+    d.device = dev;
+  }
+  return &d;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, uint32_t rank, const void* gaddr, const uint64_t* dims,
+                 const uint64_t* strides_bytes, const uint32_t* box, CUtensorMapSwizzle swizzle) {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  if (!fn) return fail(MOMMS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(map, dtype, rank, const_cast<void*>(gaddr), dims, strides_bytes, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(MOMMS_ERR_INVALID_ARG, "cuTensorMapEncodeTiled failed (%d) rank=%u dims=%llu,%llu box=%u,%u", (int)r,
+                rank, (unsigned long long)dims[0], (unsigned long long)(rank > 1 ? dims[1] : 0), box[0],
+                rank > 1 ? box[1] : 0);
+  return MOMMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Repack a strided operand into column-major scratch.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void repack_kernel(const T* __restrict__ src, int64_t rs, int64_t cs, int64_t rows, int64_t cols,
+                              T* __restrict__ dst, int64_t ld) {
+  const int64_t total = rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % rows, j = e / rows;
+    dst[i + j * ld] = src[i * rs + j * cs];
+  }
+}
+
+int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, void* dst, int64_t ld,
+                    cudaStream_t s) {
+  const int64_t total = rows * cols;
+  if (total == 0) return MOMMS_OK;
+  const int threads = 256;
+  const int blocks = (int)std::min<int64_t>(ceil_div(total, threads), 4096);
+  if (elem == 8)
+    repack_kernel<double><<<blocks, threads, 0, s>>>(static_cast<const double*>(src.ptr), src.rs, src.cs, rows, cols,
+                                                      static_cast<double*>(dst), ld);
+  else
+    repack_kernel<float><<<blocks, threads, 0, s>>>(static_cast<const float*>(src.ptr), src.rs, src.cs, rows, cols,
+                                                     static_cast<float*>(dst), ld);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "repack");
+}
+
+// ---------------------------------------------------------------------------
+// Validation and staging
+// ---------------------------------------------------------------------------
+namespace {
+
+size_t elem_size(int dtype) { return dtype == MOMMS_DTYPE_F64 ? 8 : 4; }
+
+int validate(const momms_gemm_desc* d) {
+  if (!d) return fail(MOMMS_ERR_INVALID_ARG, "desc is null");
+  if (d->dtype != MOMMS_DTYPE_F64 && d->dtype != MOMMS_DTYPE_F32)
+    return fail(MOMMS_ERR_INVALID_ARG, "unknown dtype %d", d->dtype);
+  if (d->precision < MOMMS_PREC_PLAIN || d->precision > MOMMS_PREC_SPLIT_TF32)
+    return fail(MOMMS_ERR_INVALID_ARG, "unknown precision %d", d->precision);
+  if (d->precision == MOMMS_PREC_OZAKI && d->dtype != MOMMS_DTYPE_F64)
+    return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation is an f64 mode");
+  if (d->precision == MOMMS_PREC_SPLIT_TF32 && d->dtype != MOMMS_DTYPE_F32)
+    return fail(MOMMS_ERR_UNSUPPORTED, "split-TF32 is an f32 mode");
+  if (d->precision != MOMMS_PREC_PLAIN) return fail(MOMMS_ERR_UNSUPPORTED, "precision %d not built", d->precision);
+  if (d->m < 0 || d->n < 0 || d->k < 0) return fail(MOMMS_ERR_INVALID_ARG, "negative size m=%lld n=%lld k=%lld",
+                                                    (long long)d->m, (long long)d->n, (long long)d->k);
+  if (d->m > INT32_MAX || d->n > INT32_MAX || d->k > INT32_MAX)
+    return fail(MOMMS_ERR_INVALID_ARG, "dimension above 2^31-1");
+  if (d->flags != 0) return fail(MOMMS_ERR_INVALID_ARG, "flags must be 0");
+  const momms_operand* ops[3] = {&d->a, &d->b, &d->c};
+  const int64_t rows[3] = {d->m, d->k, d->m}, cols[3] = {d->k, d->n, d->n};
+  const char* names = "ABC";
+  for (int i = 0; i < 3; ++i) {
+    if (rows[i] == 0 || cols[i] == 0) continue;
+    if (i < 2 && (d->m == 0 || d->n == 0)) continue;
+    if (!ops[i]->ptr) return fail(MOMMS_ERR_INVALID_ARG, "%c.ptr is null", names[i]);
+    if (ops[i]->rs < 0 || ops[i]->cs < 0) return fail(MOMMS_ERR_INVALID_ARG, "%c has a negative stride", names[i]);
+    if ((rows[i] > 1 && ops[i]->rs == 0) || (cols[i] > 1 && ops[i]->cs == 0))
+      return fail(MOMMS_ERR_INVALID_ARG, "%c has a zero stride", names[i]);
+    if (ops[i]->mem < MOMMS_MEM_AUTO || ops[i]->mem > MOMMS_MEM_DEVICE)
+      return fail(MOMMS_ERR_INVALID_ARG, "%c.mem is not a momms_memspace", names[i]);
+  }
+  // C must not overlap itself: the strides must separate rows and columns.
+  if (d->m > 1 && d->n > 1 && d->c.rs == d->c.cs) return fail(MOMMS_ERR_INVALID_ARG, "C has equal strides");
+  return MOMMS_OK;
+}
+
+bool is_device_ptr(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+struct Staged {
+  DevMat dev{};
+  void* owned = nullptr;
+  bool host = false;
+  int64_t rows = 0, cols = 0;
+  bool row_major = false;  // layout of the device copy
+  int64_t ld = 0;
+};
+
+// Host -> device copy of a rows x cols view into an owned buffer.
+int stage_in(const momms_operand& op, int64_t rows, int64_t cols, size_t es, bool copy, Staged& st, cudaStream_t s) {
+  st.rows = rows;
+  st.cols = cols;
+  st.host = true;
+  // column-major copy unless the source is row-major
+  st.row_major = (op.cs == 1 && op.rs != 1);
+  const int64_t inner = st.row_major ? cols : rows, outer = st.row_major ? rows : cols;
+  st.ld = round_up(std::max<int64_t>(inner, 1), 16 / (int64_t)es);
+  cudaError_t e = cudaMallocAsync(&st.owned, (size_t)st.ld * std::max<int64_t>(outer, 1) * es, s);
+  if (e != cudaSuccess) return cuda_fail(e, "staging buffer");
+  st.dev = st.row_major ? DevMat{st.owned, st.ld, 1} : DevMat{st.owned, 1, st.ld};
+  if (!copy || rows == 0 || cols == 0) return MOMMS_OK;
+  const int64_t src_inner_stride = st.row_major ? op.cs : op.rs;
+  const int64_t src_outer_stride = st.row_major ? op.rs : op.cs;
+  if (src_inner_stride == 1 && (outer == 1 || src_outer_stride >= inner)) {
+    const size_t spitch = (size_t)(outer == 1 ? inner : src_outer_stride) * es;
+    e = cudaMemcpy2DAsync(st.owned, (size_t)st.ld * es, op.ptr, spitch, (size_t)inner * es, (size_t)outer,
+                          cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "H2D copy");
+    return MOMMS_OK;
+  }
+  // general strides: gather on the host, then one copy
+  std::vector<char> tmp((size_t)st.ld * outer * es);
+  for (int64_t j = 0; j < outer; ++j)
+    for (int64_t i = 0; i < inner; ++i) {
+      const int64_t r = st.row_major ? j : i, c = st.row_major ? i : j;
+      memcpy(&tmp[((size_t)j * st.ld + i) * es], static_cast<const char*>(op.ptr) + (size_t)(r * op.rs + c * op.cs) * es,
+             es);
+    }
+  e = cudaMemcpyAsync(st.owned, tmp.data(), tmp.size(), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "H2D copy");
+  // the vector must outlive the copy
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "H2D copy");
+  return MOMMS_OK;
+}
+
+int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s) {
+  const int64_t inner = st.row_major ? st.cols : st.rows, outer = st.row_major ? st.rows : st.cols;
+  if (st.rows == 0 || st.cols == 0) return MOMMS_OK;
+  const int64_t dst_inner_stride = st.row_major ? op.cs : op.rs;
+  const int64_t dst_outer_stride = st.row_major ? op.rs : op.cs;
+  cudaError_t e;
+  if (dst_inner_stride == 1 && (outer == 1 || dst_outer_stride >= inner)) {
+    const size_t dpitch = (size_t)(outer == 1 ? inner : dst_outer_stride) * es;
+    e = cudaMemcpy2DAsync(op.ptr, dpitch, st.owned, (size_t)st.ld * es, (size_t)inner * es, (size_t)outer,
+                          cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(e, "D2H copy");
+    return MOMMS_OK;
+  }
+  std::vector<char> tmp((size_t)st.ld * outer * es);
+  e = cudaMemcpyAsync(tmp.data(), st.owned, tmp.size(), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "D2H copy");
+  for (int64_t j = 0; j < outer; ++j)
+    for (int64_t i = 0; i < inner; ++i) {
+      const int64_t r = st.row_major ? j : i, c = st.row_major ? i : j;
+      memcpy(static_cast<char*>(op.ptr) + (size_t)(r * op.rs + c * op.cs) * es, &tmp[((size_t)j * st.ld + i) * es],
+             es);
+    }
+  return MOMMS_OK;
+}
+
+int dispatch(const DevGemm& g, int precision, cudaStream_t s) {
+  (void)precision;
+  if (g.dtype == MOMMS_DTYPE_F64) return launch_dgemm_dmma(g, s);
+  return launch_sgemm_ffma(g, s);
+}
+
+}  // namespace
+
+int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
+  g_last_error[0] = 0;
+  int rc = validate(d);
+  if (rc) return rc;
+  // The reference's PartK loop runs no slab when k == 0 and leaves C as it
+  // is (src/composables/part.rs:98-106); so does this node.
+  if (d->m == 0 || d->n == 0 || d->k == 0) return MOMMS_OK;
+  if (!device_state()) return MOMMS_ERR_NO_DEVICE;
+  const size_t es = elem_size(d->dtype);
+  const momms_operand* ops[3] = {&d->a, &d->b, &d->c};
+  const int64_t rows[3] = {d->m, d->k, d->m}, cols[3] = {d->k, d->n, d->n};
+  bool host[3];
+  for (int i = 0; i < 3; ++i)
+    host[i] = ops[i]->mem == MOMMS_MEM_HOST || (ops[i]->mem == MOMMS_MEM_AUTO && !is_device_ptr(ops[i]->ptr));
+  DevGemm g;
+  g.dtype = d->dtype;
+  g.m = d->m;
+  g.n = d->n;
+  g.k = d->k;
+  g.alpha = d->alpha;
+  g.beta = d->beta;
+  Staged st[3];
+  DevMat* dm[3] = {&g.a, &g.b, &g.c};
+  for (int i = 0; i < 3; ++i) {
+    if (host[i]) {
+      const bool copy = (i < 2) || (d->beta != 0.0);
+      rc = stage_in(*ops[i], rows[i], cols[i], es, copy, st[i], s);
+      if (rc) break;
+      *dm[i] = st[i].dev;
+    } else {
+      *dm[i] = DevMat{ops[i]->ptr, ops[i]->rs, ops[i]->cs};
+    }
+  }
+  if (!rc) rc = dispatch(g, d->precision, s);
+  if (!rc && host[2]) rc = stage_out(*ops[2], es, st[2], s);
+  for (int i = 0; i < 3; ++i)
+    if (st[i].owned) cudaFreeAsync(st[i].owned, s);
+  if (host[0] || host[1] || host[2]) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "stream synchronize");
+  }
+  return rc;
+}
+
+}  // namespace momms
+
+// ---------------------------------------------------------------------------
+// extern "C" surface
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int momms_gemm(const momms_gemm_desc* desc, void* stream) {
+  return momms::gemm_impl(desc, static_cast<cudaStream_t>(stream));
+}
+
+int momms_gemm_validate(const momms_gemm_desc* desc) {
+  int rc = momms::validate(desc);
+  return rc;
+}
+
+static momms_gemm_desc make_desc(int dtype, int64_t m, int64_t n, int64_t k, double alpha, const void* a,
+                                 int64_t rs_a, int64_t cs_a, const void* b, int64_t rs_b, int64_t cs_b, double beta,
+                                 void* c, int64_t rs_c, int64_t cs_c) {
+  momms_gemm_desc d;
+  memset(&d, 0, sizeof(d));
+  d.dtype = dtype;
+  d.precision = MOMMS_PREC_PLAIN;
+  d.m = m;
+  d.n = n;
+  d.k = k;
+  d.alpha = alpha;
+  d.beta = beta;
+  d.a = momms_operand{const_cast<void*>(a), rs_a, cs_a, MOMMS_MEM_AUTO, 0};
+  d.b = momms_operand{const_cast<void*>(b), rs_b, cs_b, MOMMS_MEM_AUTO, 0};
+  d.c = momms_operand{c, rs_c, cs_c, MOMMS_MEM_AUTO, 0};
+  return d;
+}
+
+int momms_dgemm(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c, int64_t rs_c,
+                int64_t cs_c, void* stream) {
+  if (!alpha || !beta) return momms::fail(MOMMS_ERR_INVALID_ARG, "alpha/beta pointer is null");
+  momms_gemm_desc d = make_desc(MOMMS_DTYPE_F64, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c);
+  return momms::gemm_impl(&d, static_cast<cudaStream_t>(stream));
+}
+
+int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float* a, int64_t rs_a, int64_t cs_a,
+                const float* b, int64_t rs_b, int64_t cs_b, const float* beta, float* c, int64_t rs_c, int64_t cs_c,
+                void* stream) {
+  if (!alpha || !beta) return momms::fail(MOMMS_ERR_INVALID_ARG, "alpha/beta pointer is null");
+  momms_gemm_desc d = make_desc(MOMMS_DTYPE_F32, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c);
+  return momms::gemm_impl(&d, static_cast<cudaStream_t>(stream));
+}
+
+int momms_device_status(uint32_t* bits) {
+  momms::DeviceState* ds = momms::device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return momms::cuda_fail(e, "cudaDeviceSynchronize");
+  unsigned w = 0;
+  e = cudaMemcpy(&w, ds->status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(ds->status, 0, sizeof(unsigned));
+  if (e != cudaSuccess) return momms::cuda_fail(e, "status word");
+  if (bits) *bits = w;
+  if (w) return momms::fail(MOMMS_ERR_DEVICE_TIMEOUT, "device status bits 0x%x", w);
+  return MOMMS_OK;
+}
+
+const char* momms_status_string(int status) {
+  switch (status) {
+    case MOMMS_OK: return "ok";
+    case MOMMS_ERR_INVALID_ARG: return "invalid argument";
+    case MOMMS_ERR_UNSUPPORTED: return "unsupported dtype/precision combination";
+    case MOMMS_ERR_CUDA: return "CUDA runtime error";
+    case MOMMS_ERR_NO_DEVICE: return "no usable CUDA device";
+    case MOMMS_ERR_OUT_OF_MEMORY: return "device out of memory";
+    case MOMMS_ERR_DEVICE_TIMEOUT: return "a kernel's bounded wait expired";
+    case MOMMS_ERR_ADMISSION: return "request exceeds the admission budget";
+    case MOMMS_ERR_BUSY: return "busy";
+    case MOMMS_ERR_SHUTDOWN: return "server stopped";
+    default: return "unknown status";
+  }
+}
+
+const char* momms_last_error(void) { return momms::g_last_error; }
+
+int momms_abi_version(void) { return MOMMS_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// Shared device-side helpers for the momms GB300 kernels: mbarrier, TMA,
+// bounded waits, the device status word and the tile scheduler.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+namespace momms {
+
+// Device status word. A kernel whose bounded wait expires ORs one of these
+// bits in and returns; the host reads it with momms_device_status().
+enum : unsigned {
+  DEV_OK = 0u,
+  DEV_TIMEOUT_FULL = 1u,   // consumer gave up waiting for a TMA stage
+  DEV_TIMEOUT_EMPTY = 2u,  // producer gave up waiting for a free stage
+  DEV_TIMEOUT_MMA = 4u,    // epilogue gave up waiting for the tensor core
+  DEV_BAD_CONFIG = 8u,     // launch shape does not match the kernel
+};
+
+// Upper bound on polls of one mbarrier wait. A healthy pipeline completes a
+// wait within microseconds; this limit (~seconds) only ends a stuck kernel.
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+__host__ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on phase `parity`. Returns false when the limit expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+  return false;
+}
+
+// 2-D tiled TMA load global -> shared, completing on an mbarrier.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, uint64_t* bar, int32_t c0,
+                                            int32_t c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// 3-D variant (used for operand stacks such as slice planes).
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, uint64_t* bar, int32_t c0,
+                                            int32_t c1, int32_t c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(smem_u32(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+__device__ __forceinline__ void report_status(unsigned* status, unsigned bit) {
+  if (status) atomicOr(status, bit);
+}
+
+// Persistent tile scheduler over (m-tiles x n-tiles x k-splits) work units.
+// Units are numbered split-major inside each output tile so that the splits
+// of one tile run close together in time; output tiles are visited in
+// groups of `group_m` m-tiles for L2 reuse of the B panel.
+struct TileSched {
+  int tiles_m, tiles_n, splits, group_m;
+  int64_t k_per_split;  // multiple of the kernel's BK
+  __host__ __device__ int64_t units() const { return (int64_t)tiles_m * tiles_n * splits; }
+  __device__ void decode(int64_t u, int& tm, int& tn, int& split) const {
+    split = (int)(u % splits);
+    int64_t t = u / splits;
+    int64_t per_group = (int64_t)group_m * tiles_n;
+    int64_t g = t / per_group;
+    int64_t r = t % per_group;
+    int first_m = (int)(g * group_m);
+    int gm = min(group_m, tiles_m - first_m);
+    tm = first_m + (int)(r % gm);
+    tn = (int)(r / gm);
+  }
+};
+
+}  // namespace momms

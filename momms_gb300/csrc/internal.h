@@ -1,0 +1,62 @@
+// Host-side internals shared by the momms GB300 translation units.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/momms_gpu.h"
+
+namespace momms {
+
+// Per-device state created on first use.
+struct DeviceState {
+  int device = -1;
+  int sm_count = 0;
+  unsigned* status = nullptr;  // device status word (see DEV_* bits)
+};
+
+// Returns the state of the calling thread's current device (initialising it
+// on first use), or nullptr with the error recorded.
+DeviceState* device_state();
+
+// Record an error message for momms_last_error() and return `code`.
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so that the
+// library does not link libcuda directly.
+int encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, uint32_t rank, const void* gaddr,
+                 const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box,
+                 CUtensorMapSwizzle swizzle);
+
+// A device-resident operand as the kernels see it: element (i, j) is at
+// ptr[i * rs + j * cs].
+struct DevMat {
+  void* ptr;
+  int64_t rs, cs;
+};
+
+// One GEMM with all operands already on the device.
+struct DevGemm {
+  int dtype;  // momms_dtype
+  int64_t m, n, k;
+  double alpha, beta;
+  DevMat a, b, c;
+};
+
+// Launchers for the plain paths (device operands; asynchronous on `s`).
+int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s);
+int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s);
+
+// Copy an operand into a column-major device scratch matrix with an even
+// leading dimension (used when its strides or alignment do not suit TMA or
+// vector loads). `dst` must hold rows * round_up(ld) elements.
+int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, void* dst, int64_t ld,
+                    cudaStream_t s);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+}  // namespace momms

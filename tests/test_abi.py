@@ -1,0 +1,100 @@
+"""The C ABI library, checked without a GPU: it loads, exports every function
+that include/*.h declares, and rejects bad descriptors before touching the
+device."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+import momms_gb300 as mg
+from tests import gpu_util as gu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(mg.LIB_PATH):
+        from momms_gb300 import build as b
+        b.build()
+    return mg.load_library()
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(momms_\w+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 8
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version(lib):
+    assert lib.momms_abi_version() == 1
+
+
+def test_status_strings(lib):
+    for code in range(0, 10):
+        s = lib.momms_status_string(code).decode()
+        assert s and s != "unknown status"
+    assert lib.momms_status_string(12345).decode() == "unknown status"
+
+
+def _desc(**kw):
+    d = gu.make_desc(mg.DTYPE_F64, 4, 5, 6, 1.0, 1.0, (8, 1, 4), (8, 1, 6), (8, 1, 4))
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def test_validate_accepts_good_desc(lib):
+    assert lib.momms_gemm_validate(ctypes.byref(_desc())) == mg.OK
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("m", -1, mg.ERR_INVALID_ARG),
+    ("k", -5, mg.ERR_INVALID_ARG),
+    ("dtype", 7, mg.ERR_INVALID_ARG),
+    ("precision", 9, mg.ERR_INVALID_ARG),
+    ("flags", 1, mg.ERR_INVALID_ARG),
+    ("m", 2**31, mg.ERR_INVALID_ARG),
+])
+def test_validate_rejects(lib, field, value, code):
+    assert lib.momms_gemm_validate(ctypes.byref(_desc(**{field: value}))) == code
+
+
+def test_validate_rejects_null_and_bad_strides(lib):
+    d = _desc()
+    d.a = mg.Operand(None, 1, 4, 0, 0)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_INVALID_ARG
+    d = _desc()
+    d.c = mg.Operand(8, 3, 3, 0, 0)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_INVALID_ARG
+    d = _desc()
+    d.b = mg.Operand(8, -1, 6, 0, 0)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_INVALID_ARG
+    d = _desc()
+    d.a = mg.Operand(8, 1, 4, 5, 0)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_INVALID_ARG
+    assert lib.momms_gemm_validate(None) == mg.ERR_INVALID_ARG
+
+
+def test_validate_mode_dtype_pairs(lib):
+    d = _desc(dtype=mg.DTYPE_F32, precision=mg.PREC_OZAKI)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_UNSUPPORTED
+    d = _desc(dtype=mg.DTYPE_F64, precision=mg.PREC_SPLIT_TF32)
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_UNSUPPORTED
+
+
+def test_last_error_message(lib):
+    lib.momms_gemm_validate(ctypes.byref(_desc(m=-1)))
+    assert b"negative" in lib.momms_last_error()
