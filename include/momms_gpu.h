@@ -118,6 +118,17 @@ const char* momms_last_error(void);
 /* ABI version of the loaded library (MOMMS_ABI_VERSION at build time). */
 int momms_abi_version(void);
 
+/* Number of kernels this library has launched in this process (all devices).
+ * No reference counterpart: evidence for benchmarks of what ran on the GPU. */
+unsigned long long momms_launch_count(void);
+
+/* Measures the current device's peak issue rate in TFLOP/s with a
+ * register-only loop: kind 0 = FP64 tensor-core MMA (DMMA m8n8k4),
+ * kind 1 = FP32 FFMA. The roofline denominators of the f64 and f32 plain
+ * paths. No reference counterpart (the reference only reports GFLOP/s,
+ * src/util.rs:94-97). Synchronises the device. */
+int momms_measure_peak(int kind, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,10 @@ def load_library(path=None):
     lib.momms_last_error.restype = ctypes.c_char_p
     lib.momms_abi_version.argtypes = []
     lib.momms_abi_version.restype = i32
+    lib.momms_launch_count.argtypes = []
+    lib.momms_launch_count.restype = ctypes.c_ulonglong
+    lib.momms_measure_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+    lib.momms_measure_peak.restype = i32
     if path is None:
         _lib = lib
     return lib

@@ -118,6 +118,7 @@ int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, 
   else
     repack_kernel<float><<<blocks, threads, 0, s>>>(static_cast<const float*>(src.ptr), src.rs, src.cs, rows, cols,
                                                      static_cast<float*>(dst), ld);
+  note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "repack");
 }

@@ -368,6 +368,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
     kern<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+    note_launch();
     return cudaGetLastError();
   };
   if (oa == ORIENT_XC && ob == ORIENT_XC) ce = launch(dgemm_kernel<true, true>);

@@ -56,6 +56,9 @@ int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s);
 int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, void* dst, int64_t ld,
                     cudaStream_t s);
 
+// Counts kernel launches made by this library (momms_launch_count()).
+void note_launch(int n = 1);
+
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
 

@@ -268,6 +268,7 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
     if (vec) sgemm_kernel<false, false, true><<<grid, THREADS, 0, s>>>(p);
     else sgemm_kernel<false, false, false><<<grid, THREADS, 0, s>>>(p);
   }
+  note_launch();
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_fail(ce, "sgemm_ffma launch");
   if (ws) cudaFreeAsync(ws, s);
