@@ -101,6 +101,34 @@ int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float
                 const float* b, int64_t rs_b, int64_t cs_b, const float* beta, float* c, int64_t rs_c,
                 int64_t cs_c, void* stream);
 
+/* f64 GEMM that allocates no memory, for callers that cannot: an application
+ * whose device memory is already owned by its own pool or framework (a
+ * cudaMalloc from this library would fail or compete with it), or a
+ * latency-critical loop that cannot afford cudaMalloc / cudaFree, their
+ * implicit device-wide synchronisation or an out-of-memory failure midway.
+ * No counterpart in the reference (its packing buffers are heap allocations,
+ * src/composables/pack.rs:336-344).
+ *
+ * Same arguments, same kernel and same tile / split-k plan as momms_dgemm, but
+ * all of A, B and C must already be device memory, and A and B must each have
+ * unit stride along one index with the other stride a multiple of 2 elements
+ * and a 16-byte aligned base (other layouts would need a repack copy). The
+ * split-k scratch is one device-global array of MOMMS_NOALLOC_SCRATCH_BYTES
+ * (160 partial tiles of 128 x 128 doubles plus 1024 tile counters) that every
+ * GPU loading this library holds until the process exits; a problem whose
+ * split-k plan needs more than that is rejected with MOMMS_ERR_INVALID_ARG.
+ * All calls on a device share that array and it keeps the last call's
+ * contents, so calls that overlap on the GPU (other streams, or other host
+ * threads) race and must be serialised by the caller. The first call on each
+ * device runs a one-time set-up with that device current (it looks up the
+ * array's device address); make that first call before any stream capture.
+ * A kernel whose bounded wait expires stops early without recording a status
+ * here. Asynchronous on `stream`. */
+#define MOMMS_NOALLOC_SCRATCH_BYTES 20975616
+int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a,
+                        int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
+                        int64_t rs_c, int64_t cs_c, void* stream);
+
 /* Checks a descriptor without touching the GPU: sizes, strides, enums.
  * Returns MOMMS_OK or MOMMS_ERR_INVALID_ARG / MOMMS_ERR_UNSUPPORTED. */
 int momms_gemm_validate(const momms_gemm_desc* desc);

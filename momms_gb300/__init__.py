@@ -78,6 +78,9 @@ def load_library(path=None):
         P = ctypes.POINTER(ct)
         f.argtypes = [i64, i64, i64, P, vp, i64, i64, vp, i64, i64, P, vp, i64, i64, vp]
         f.restype = i32
+    Pd = ctypes.POINTER(ctypes.c_double)
+    lib.momms_dgemm_noalloc.argtypes = [i64, i64, i64, Pd, vp, i64, i64, vp, i64, i64, Pd, vp, i64, i64, vp]
+    lib.momms_dgemm_noalloc.restype = i32
     lib.momms_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
     lib.momms_device_status.restype = i32
     lib.momms_status_string.argtypes = [i32]

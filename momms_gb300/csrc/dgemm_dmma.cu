@@ -383,3 +383,183 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
 }
 
 }  // namespace momms
+
+// ---------------------------------------------------------------------------
+// momms_dgemm_noalloc: the f64 GEMM for callers that cannot allocate device
+// memory. Same kernel and same tile / split-k plan as momms_dgemm on device
+// operands; the split-k scratch comes from a fixed device-global array instead
+// of the stream-ordered pool.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace momms {
+namespace {
+
+constexpr size_t kNoallocPartialTiles = 160;  // 128 x 128 f64 partial tiles
+constexpr size_t kNoallocPartialBytes = kNoallocPartialTiles * dmma::BM * dmma::BN * sizeof(double);
+constexpr size_t kNoallocCounterSlots = 1024;  // per-output-tile arrival counters
+static_assert(kNoallocPartialBytes + kNoallocCounterSlots * sizeof(unsigned) == MOMMS_NOALLOC_SCRATCH_BYTES,
+              "scratch layout must match MOMMS_NOALLOC_SCRATCH_BYTES");
+
+// The scratch itself. Every GPU that loads this library holds these bytes
+// until the process exits; every call of momms_dgemm_noalloc on a device uses
+// the same bytes. In host code this name is only a stand-in for the device
+// address: host code passes the address from cudaGetSymbolAddress instead.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MOMMS_NOALLOC_SCRATCH_BYTES];
+
+struct NoallocDevice {
+  bool ready = false;
+  void* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+  int sm_count = 0;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[64];
+
+// One-time set-up per device, run by the first call on that device with the
+// device current: looks up the scratch array's device address and the SM
+// count, and raises the kernels' shared-memory limit. Allocates nothing.
+int noalloc_setup(NoallocDevice*& out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(MOMMS_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoallocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    const void* kerns[4] = {(const void*)dmma::dgemm_kernel<true, true>, (const void*)dmma::dgemm_kernel<true, false>,
+                            (const void*)dmma::dgemm_kernel<false, true>, (const void*)dmma::dgemm_kernel<false, false>};
+    for (const void* kf : kerns) {
+      e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, dmma::SMEM_BYTES);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+    }
+    d.scratch = p;
+    d.sm_count = sms;
+    d.ready = true;
+  }
+  out = &d;
+  return MOMMS_OK;
+}
+
+}  // namespace
+}  // namespace momms
+
+extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a,
+                                   int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b,
+                                   const double* beta, double* c, int64_t rs_c, int64_t cs_c, void* stream) {
+  using namespace momms;
+  using namespace momms::dmma;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!alpha || !beta) return fail(MOMMS_ERR_INVALID_ARG, "alpha/beta pointer is null");
+  if (m < 0 || n < 0 || k < 0) return fail(MOMMS_ERR_INVALID_ARG, "negative size");
+  if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX) return fail(MOMMS_ERR_INVALID_ARG, "dimension above 2^31-1");
+  if (m == 0 || n == 0 || k == 0) return MOMMS_OK;  // as momms_dgemm: k == 0 leaves C as it is
+  if (!a || !b || !c) return fail(MOMMS_ERR_INVALID_ARG, "null operand pointer");
+  if (rs_a < 0 || cs_a < 0 || rs_b < 0 || cs_b < 0 || rs_c < 0 || cs_c < 0)
+    return fail(MOMMS_ERR_INVALID_ARG, "negative stride");
+  if (m > 1 && n > 1 && rs_c == cs_c) return fail(MOMMS_ERR_INVALID_ARG, "C has equal strides");
+  const void* ptrs[3] = {a, b, c};
+  for (const void* p : ptrs) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess ||
+        !(at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)) {
+      cudaGetLastError();
+      return fail(MOMMS_ERR_INVALID_ARG,
+                  "momms_dgemm_noalloc takes device operands only (staging host memory would allocate)");
+    }
+  }
+  NoallocDevice* nd = nullptr;
+  int rc = noalloc_setup(nd);
+  if (rc) return rc;
+
+  DevGemm g;
+  g.dtype = MOMMS_DTYPE_F64;
+  g.m = m; g.n = n; g.k = k;
+  g.alpha = *alpha; g.beta = *beta;
+  g.a = DevMat{const_cast<double*>(a), rs_a, cs_a};
+  g.b = DevMat{const_cast<double*>(b), rs_b, cs_b};
+  g.c = DevMat{c, rs_c, cs_c};
+  const Orient oa = pick_orient(g.a, g.m, g.k, true, 8);
+  const Orient ob = pick_orient(g.b, g.k, g.n, false, 8);
+  if (oa == ORIENT_REPACK || ob == ORIENT_REPACK)
+    return fail(MOMMS_ERR_INVALID_ARG,
+                "momms_dgemm_noalloc needs A and B with unit stride along one index, the other stride a multiple of "
+                "2 elements and 16-byte aligned bases (other layouts need a repack copy, which would allocate)");
+
+  CUtensorMap tmA, tmB;
+  {
+    uint64_t dims[2], strides[1];
+    uint32_t box[2];
+    if (oa == ORIENT_XC) {
+      dims[0] = g.m; dims[1] = g.k;
+      strides[0] = (uint64_t)(g.k == 1 ? round_up(g.m * 8, 16) : g.a.cs * 8);
+      box[0] = 16; box[1] = BK;
+    } else {
+      dims[0] = g.k; dims[1] = g.m;
+      strides[0] = (uint64_t)(g.m == 1 ? round_up(g.k * 8, 16) : g.a.rs * 8);
+      box[0] = BK; box[1] = BM;
+    }
+    rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, g.a.ptr, dims, strides, box,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    if (ob == ORIENT_XC) {
+      dims[0] = g.n; dims[1] = g.k;
+      strides[0] = (uint64_t)(g.k == 1 ? round_up(g.n * 8, 16) : g.b.rs * 8);
+      box[0] = 16; box[1] = BK;
+    } else {
+      dims[0] = g.k; dims[1] = g.n;
+      strides[0] = (uint64_t)(g.n == 1 ? round_up(g.k * 8, 16) : g.b.cs * 8);
+      box[0] = BK; box[1] = BN;
+    }
+    rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, g.b.ptr, dims, strides, box,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+  }
+
+  // The same tile / split-k plan as momms_dgemm, so both give the same result.
+  Params p;
+  p.m = g.m; p.n = g.n; p.k = g.k;
+  p.alpha = g.alpha; p.beta = g.beta;
+  p.c = c;
+  p.rsc = rs_c; p.csc = cs_c;
+  p.status = nullptr;  // no status word here: that one is allocated on first use
+  const int tiles_m = (int)ceil_div(g.m, BM), tiles_n = (int)ceil_div(g.n, BN);
+  const int64_t tiles = (int64_t)tiles_m * tiles_n;
+  const int64_t kblocks = ceil_div(g.k, BK);
+  int splits = 1;
+  if (tiles < nd->sm_count) {
+    splits = (int)std::min<int64_t>(nd->sm_count / tiles, kblocks / 8);
+    splits = std::max(1, std::min(splits, 32));
+  }
+  const int64_t kb_split = ceil_div(kblocks, splits);
+  splits = (int)ceil_div(kblocks, kb_split);
+  p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};
+  p.partials = nullptr;
+  p.counters = nullptr;
+  if (splits > 1) {
+    if ((size_t)(tiles * splits) > kNoallocPartialTiles || (size_t)tiles > kNoallocCounterSlots)
+      return fail(MOMMS_ERR_INVALID_ARG,
+                  "this problem needs %lld split-k partial tiles of 128x128 doubles; the no-alloc scratch holds %zu "
+                  "(%d bytes)",
+                  (long long)(tiles * splits), kNoallocPartialTiles, (int)MOMMS_NOALLOC_SCRATCH_BYTES);
+    p.partials = static_cast<double*>(nd->scratch);
+    p.counters = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(nd->scratch) + kNoallocPartialBytes);
+    // counters must start at zero; the array keeps whatever the last call left
+    cudaError_t e = cudaMemsetAsync(p.counters, 0, (size_t)tiles * sizeof(unsigned), s);
+    if (e != cudaSuccess) return cuda_fail(e, "clear split-k counters");
+  }
+  const int grid = (int)std::min<int64_t>(p.sched.units(), nd->sm_count);
+  if (oa == ORIENT_XC && ob == ORIENT_XC) dgemm_kernel<true, true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+  else if (oa == ORIENT_XC) dgemm_kernel<true, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+  else if (ob == ORIENT_XC) dgemm_kernel<false, true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+  else dgemm_kernel<false, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "dgemm_noalloc launch");
+  return MOMMS_OK;
+}
