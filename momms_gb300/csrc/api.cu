@@ -140,7 +140,10 @@ int validate(const momms_gemm_desc* d) {
     return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation is an f64 mode");
   if (d->precision == MOMMS_PREC_SPLIT_TF32 && d->dtype != MOMMS_DTYPE_F32)
     return fail(MOMMS_ERR_UNSUPPORTED, "split-TF32 is an f32 mode");
-  if (d->precision != MOMMS_PREC_PLAIN) return fail(MOMMS_ERR_UNSUPPORTED, "precision %d not built", d->precision);
+  if (d->precision == MOMMS_PREC_OZAKI && (d->slices < 0 || d->slices > 16))
+    return fail(MOMMS_ERR_INVALID_ARG, "Ozaki slice count %d outside 0..16", d->slices);
+  if (d->precision == MOMMS_PREC_OZAKI && !(d->target_rel_err >= 0.0 && d->target_rel_err < 1.0))
+    return fail(MOMMS_ERR_INVALID_ARG, "target_rel_err must be in [0, 1)");
   if (d->m < 0 || d->n < 0 || d->k < 0) return fail(MOMMS_ERR_INVALID_ARG, "negative size m=%lld n=%lld k=%lld",
                                                     (long long)d->m, (long long)d->n, (long long)d->k);
   if (d->m > INT32_MAX || d->n > INT32_MAX || d->k > INT32_MAX)
@@ -246,9 +249,15 @@ int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t
   return MOMMS_OK;
 }
 
-int dispatch(const DevGemm& g, int precision, cudaStream_t s) {
-  (void)precision;
-  if (g.dtype == MOMMS_DTYPE_F64) return launch_dgemm_dmma(g, s);
+int dispatch(const DevGemm& g, const momms_gemm_desc* d, cudaStream_t s) {
+  if (g.dtype == MOMMS_DTYPE_F64) {
+    if (d->precision == MOMMS_PREC_OZAKI) {
+      int used = 0;
+      return launch_dgemm_ozaki(g, d->target_rel_err, d->slices, &used, s);
+    }
+    return launch_dgemm_dmma(g, s);
+  }
+  if (d->precision == MOMMS_PREC_SPLIT_TF32) return launch_sgemm_tf32x3(g, s);
   return launch_sgemm_ffma(g, s);
 }
 
@@ -287,7 +296,7 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
       *dm[i] = DevMat{ops[i]->ptr, ops[i]->rs, ops[i]->cs};
     }
   }
-  if (!rc) rc = dispatch(g, d->precision, s);
+  if (!rc) rc = dispatch(g, d, s);
   if (!rc && host[2]) rc = stage_out(*ops[2], es, st[2], s);
   for (int i = 0; i < 3; ++i)
     if (st[i].owned) cudaFreeAsync(st[i].owned, s);

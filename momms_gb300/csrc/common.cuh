@@ -21,7 +21,7 @@ enum : unsigned {
 
 // Upper bound on polls of one mbarrier wait. A healthy pipeline completes a
 // wait within microseconds; this limit (~seconds) only ends a stuck kernel.
-constexpr uint32_t kWaitLimit = 1u << 26;
+constexpr uint32_t kWaitLimit = 1u << 24;
 
 __host__ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -49,6 +49,10 @@ struct DevGemm {
 // Launchers for the plain paths (device operands; asynchronous on `s`).
 int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s);
 int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s);
+int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s);
+// Ozaki FP64 emulation: target relative error (0 = FP64 level) and slice count
+// (0 = chosen from the target). *slices_used receives the count actually used.
+int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int* slices_used, cudaStream_t s);
 
 // Copy an operand into a column-major device scratch matrix with an even
 // leading dimension (used when its strides or alignment do not suit TMA or

@@ -1,0 +1,359 @@
+// FP64 GEMM emulated on the fp16 tensor cores (Ozaki scheme, slice products).
+//
+// Ozaki, Ogita, Oishi, Rump (2012): scale each row of A (column of B) by a
+// power of two so that its entries lie in (-1, 1), split every scaled entry
+// into s signed digits of `bits` bits,
+//     x = 2^e * sum_{t=1..s} d_t 2^(-bits*t),   d_t integers, |d_t| <= 2^bits,
+// and form A*B from digit-plane products A_t * B_u, each exact in a
+// wide-enough accumulator. Products on the same anti-diagonal d = t + u share
+// the weight 2^(-bits*d); the scheme keeps d <= s + 1 (triangular truncation).
+//
+// GB300 form (sm_103a has no integer tcgen05 kind): digits are fp16 values
+// (exact for |d| <= 2048), the products run on tcgen05 kind::f16 with FP32
+// accumulation in TMEM, and every accumulation chunk is kept below 2^22 so
+// that it is an exact integer; chunks are gathered in int32 registers, and the
+// diagonals are combined in FP64 by Horner's rule in the epilogue
+// (R = S_d + 2^-bits R, from the smallest weight up), so FP64 arithmetic is
+// used only for the exponent scaling and this recombination. See
+// slicegemm.cuh for the engine.
+//
+// The slice count is chosen per call from the requested componentwise error
+// (|dC_ij| / (|A||B|)_ij) with a bound evaluated on sampled entries: with RN
+// digits the truncation error is at most
+//   2^(-bits*s-1) * (2^e_i sum_p |b_pj| + 2^f_j sum_p |a_ip|
+//                    + (s-1)/2 * k * 2^(e_i+f_j))
+// (digit truncation of A and B, then the largest dropped diagonal).
+#include <cuda_fp16.h>
+#include <math.h>
+
+#include "internal.h"
+#include "planes.cuh"
+#include "slicegemm.cuh"
+
+namespace momms {
+
+namespace {
+
+constexpr int kDigitBits = 7;
+
+// Exponent e with max_p |x(r,p)| < 2^e (frexp); 0 for an all-zero row;
+// INT32_MAX when the row holds a NaN or an infinity.
+__global__ void __launch_bounds__(256) row_exp_kernel(const double* __restrict__ x, int64_t sr, int64_t sp, int64_t R,
+                                                      int64_t K, bool r_contig, int* __restrict__ exps) {
+  __shared__ double red[8][33];
+  __shared__ int bad[8][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  if (r_contig) {
+    // threads along r (the contiguous index), ty strides over p
+    const int64_t r = r0 + tx;
+    double mx = 0.0;
+    int nf = 0;
+    if (r < R)
+      for (int64_t pp = ty; pp < K; pp += 8) {
+        const double v = x[r * sr + pp * sp];
+        nf |= !isfinite(v);
+        mx = fmax(mx, fabs(v));
+      }
+    red[ty][tx] = mx;
+    bad[ty][tx] = nf;
+    __syncthreads();
+    if (ty == 0 && r < R) {
+      for (int i = 1; i < 8; ++i) {
+        mx = fmax(mx, red[i][tx]);
+        nf |= bad[i][tx];
+      }
+      int e = 0;
+      if (!nf && mx > 0.0) frexp(mx, &e);
+      exps[r] = nf ? INT32_MAX : e;
+    }
+  } else {
+    // one warp per row, lanes along p
+    for (int i = 0; i < 4; ++i) {
+      const int64_t r = r0 + ty + 8 * i;
+      if (r >= R) break;
+      double mx = 0.0;
+      int nf = 0;
+      for (int64_t pp = tx; pp < K; pp += 32) {
+        const double v = x[r * sr + pp * sp];
+        nf |= !isfinite(v);
+        mx = fmax(mx, fabs(v));
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+      }
+      if (tx == 0) {
+        int e = 0;
+        if (!nf && mx > 0.0) frexp(mx, &e);
+        exps[r] = nf ? INT32_MAX : e;
+      }
+    }
+  }
+}
+
+struct OzakiSliceOp {
+  using Tout = __half;
+  const int* exps;
+  int slices;
+  int bits;
+  __device__ __forceinline__ void operator()(double v, int64_t r, __half* out, int64_t plane_elems) const {
+    const int e = exps[r];
+    double x = (e == INT32_MAX) ? 0.0 : ldexp(v, -e);
+    const double up = (double)(1 << bits);
+    for (int t = 0; t < slices; ++t) {
+      const double y = x * up;  // exact (power of two)
+      const double d = rint(y);
+      x = y - d;  // exact: |y - rint(y)| <= 1/2
+      out[(int64_t)t * plane_elems] = __double2half(d);
+    }
+  }
+};
+
+// Sampled quantities for the slice-count bound: for sampled (i, j),
+//   q1 = (2^e_i sum|b_.j| + 2^f_j sum|a_i.|) / (|A||B|)_ij
+//   q2 = k 2^(e_i+f_j) / (|A||B|)_ij
+// reduced to their maxima in out[0], out[1] (as ordered non-negative floats).
+__global__ void sample_bound_kernel(const double* __restrict__ a, int64_t rsa, int64_t csa,
+                                    const double* __restrict__ b, int64_t rsb, int64_t csb, int64_t m, int64_t n,
+                                    int64_t k, const int* __restrict__ rexp, const int* __restrict__ cexp,
+                                    int samples, unsigned long long* out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= samples) return;
+  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(warp + 1);
+  h ^= h >> 31;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 29;
+  const int64_t i = (int64_t)(h % (uint64_t)m);
+  const int64_t j = (int64_t)((h >> 20) % (uint64_t)n);
+  double sab = 0.0, sa = 0.0, sb = 0.0;
+  for (int64_t pp = lane; pp < k; pp += 32) {
+    const double av = fabs(a[i * rsa + pp * csa]);
+    const double bv = fabs(b[pp * rsb + j * csb]);
+    sab += av * bv;
+    sa += av;
+    sb += bv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sab += __shfl_xor_sync(0xffffffffu, sab, o);
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  if (lane == 0) {
+    const int ei = rexp[i], fj = cexp[j];
+    if (ei == INT32_MAX || fj == INT32_MAX || sab == 0.0) return;
+    const double q1 = (ldexp(sb, ei) + ldexp(sa, fj)) / sab;
+    const double q2 = ldexp((double)k, ei + fj) / sab;
+    // non-negative doubles order like their bit patterns
+    atomicMax(&out[0], (unsigned long long)__double_as_longlong(q1));
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(q2));
+  }
+}
+
+// FP64 recombination of the exact group sums (Horner from the smallest
+// weight): R = S_g + w_g R with w_g = 2^-bits at the first group of a new
+// diagonal and 1 inside a split diagonal; then
+// C = beta*C + alpha * 2^(e_i + f_j - 2 bits) * R.
+struct CombineParams {
+  const int* sbuf;
+  int64_t plane;
+  int ngroups;
+  uint8_t shift[sp::MAX_GROUPS];
+  int64_t m, n;
+  const int* row_exp;
+  const int* col_exp;
+  int bits;
+  double alpha, beta;
+  double* c;
+  int64_t rsc, csc;
+};
+
+__global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
+  const int64_t total = p.m * p.n;
+  const double down = ldexp(1.0, -p.bits);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % p.m, j = e / p.m;
+    double R = 0.0;
+    for (int g = 0; g < p.ngroups; ++g) R = fma(p.shift[g] ? down : 1.0, R, (double)p.sbuf[g * p.plane + e]);
+    const int er = p.row_exp[i], ec = p.col_exp[j];
+    double v;
+    if (er == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
+    else v = ldexp(R, er + ec - 2 * p.bits);
+    double* cp = p.c + i * p.rsc + j * p.csc;
+    const double sv = v * p.alpha;
+    *cp = (p.beta == 0.0) ? sv : fma(p.beta, *cp, sv);
+  }
+}
+
+// Worst-case componentwise error of an s-slice product, relative to |A||B|.
+double ozaki_bound(int s, int bits, double q1, double q2) {
+  return ldexp(1.0, -bits * s - 1) * (q1 + 0.5 * (s - 1) * q2);
+}
+
+}  // namespace
+
+int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
+  DeviceState* ds = device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  const int bits = kDigitBits;
+  const int64_t m = g.m, n = g.n, k = g.k;
+  cudaError_t ce;
+
+  int* exps = nullptr;
+  if ((ce = cudaMallocAsync(&exps, (size_t)(m + n) * sizeof(int), s)) != cudaSuccess)
+    return cuda_fail(ce, "Ozaki exponents");
+  int* rexp = exps;
+  int* cexp = exps + m;
+  const double* A = static_cast<const double*>(g.a.ptr);
+  const double* B = static_cast<const double*>(g.b.ptr);
+  {
+    // A viewed as m x k; B viewed transposed, n x k
+    const bool a_rc = (g.a.rs == 1 && g.a.cs != 1), b_rc = (g.b.cs == 1 && g.b.rs != 1);
+    row_exp_kernel<<<(unsigned)ceil_div(m, 32), dim3(32, 8), 0, s>>>(A, g.a.rs, g.a.cs, m, k, a_rc, rexp);
+    row_exp_kernel<<<(unsigned)ceil_div(n, 32), dim3(32, 8), 0, s>>>(B, g.b.cs, g.b.rs, n, k, b_rc, cexp);
+    note_launch(2);
+  }
+
+  int ns = slices;
+  if (ns <= 0) {
+    // choose from the target with the sampled bound
+    const double tgt = target > 0.0 ? target : ldexp(1.0, -52);
+    unsigned long long* q = nullptr;
+    if ((ce = cudaMallocAsync(&q, 2 * sizeof(unsigned long long), s)) != cudaSuccess)
+      return cuda_fail(ce, "Ozaki bound sample");
+    cudaMemsetAsync(q, 0, 2 * sizeof(unsigned long long), s);
+    const int samples = 2048;
+    sample_bound_kernel<<<samples / 8, 256, 0, s>>>(A, g.a.rs, g.a.cs, B, g.b.rs, g.b.cs, m, n, k, rexp, cexp,
+                                                    samples, q);
+    note_launch();
+    unsigned long long hq[2] = {0, 0};
+    ce = cudaMemcpyAsync(hq, q, sizeof(hq), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    cudaFreeAsync(q, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
+    double q1, q2;
+    memcpy(&q1, &hq[0], 8);
+    memcpy(&q2, &hq[1], 8);
+    if (!(q1 > 0.0)) q1 = 4.0;  // no usable sample (zero operands): nominal uniform-data value
+    if (!(q2 > 0.0)) q2 = 4.0;
+    ns = 1;
+    while (ns < 16 && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
+  }
+  if (slices_used) *slices_used = ns;
+
+  const int64_t kp = round_up(k, 8);  // 16-byte rows of fp16
+  const size_t a_plane = (size_t)m * kp, b_plane = (size_t)n * kp;
+  __half* planes_buf = nullptr;
+  if ((ce = cudaMallocAsync(&planes_buf, (size_t)ns * (a_plane + b_plane) * sizeof(__half), s)) != cudaSuccess)
+    return cuda_fail(ce, "Ozaki slice planes");
+  __half* pa = planes_buf;
+  __half* pb = planes_buf + (size_t)ns * a_plane;
+  planes::launch_to_planes(A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, OzakiSliceOp{rexp, ns, bits}, s);
+  planes::launch_to_planes(B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, OzakiSliceOp{cexp, ns, bits}, s);
+  note_launch(2);
+
+  if (k > 65536) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 (int32 digit sums)");
+  CUtensorMap tmA, tmB;
+  {
+    uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)ns};
+    uint64_t strides[2] = {(uint64_t)kp * 2, (uint64_t)a_plane * 2};
+    uint32_t box[3] = {64, (uint32_t)sp::BM, 1};
+    int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)ns};
+    uint64_t stridesb[2] = {(uint64_t)kp * 2, (uint64_t)b_plane * 2};
+    uint32_t boxb[3] = {64, (uint32_t)sp::BN, 1};
+    rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+  }
+
+  sp::Params p;
+  memset(&p, 0, sizeof(p));
+  p.m = m;
+  p.n = n;
+  p.kelems = 64;
+  p.kblocks = (int)ceil_div(k, 64);
+  p.tiles_m = (int)ceil_div(m, sp::BM);
+  p.tiles_n = (int)ceil_div(n, sp::BN);
+  CombineParams cp;
+  memset(&cp, 0, sizeof(cp));
+  // Diagonals from the smallest weight (d = ns+1) to the largest (d = 2). A
+  // diagonal whose int32 sums could pass 2^30 is split into several groups
+  // of whole pairs; only the first group of a diagonal shifts R by 2^-bits.
+  int np = 0, ng = 0;
+  for (int gi = 0; gi < ns; ++gi) {
+    const int d = ns + 1 - gi;  // digit indices t, u in 1..ns with t + u = d
+    int tlist[16], nt = 0;
+    double maxprod = 0.0;
+    for (int t = 1; t <= ns; ++t) {
+      const int u = d - t;
+      if (u < 1 || u > ns) continue;
+      tlist[nt++] = t;
+      const double bt = ldexp(1.0, t == 1 ? bits : bits - 1), bu = ldexp(1.0, u == 1 ? bits : bits - 1);
+      maxprod = fmax(maxprod, bt * bu);
+    }
+    // every TMEM chunk keeps |sum| <= 2^22 (exact in FP32, and inside the
+    // magic-constant conversion range)
+    const int chunk = (int)std::max<int64_t>(1, (int64_t)(ldexp(1.0, 22) / maxprod) / 64);
+    // pairs per group so that the int32 group sums stay below 2^30
+    const double per_pair = (double)p.kblocks * 64.0 * maxprod;
+    const int pairs_per_group = (int)std::max(1.0, floor(ldexp(1.0, 30) / per_pair));
+    for (int i0 = 0; i0 < nt; i0 += pairs_per_group) {
+      if (ng >= sp::MAX_GROUPS) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
+      p.group_begin[ng] = np;
+      p.chunk_kb[ng] = chunk;
+      cp.shift[ng] = (i0 == 0 && ng > 0) ? 1 : 0;
+      for (int i = i0; i < std::min(nt, i0 + pairs_per_group); ++i) {
+        p.pair_a[np] = (uint8_t)(tlist[i] - 1);
+        p.pair_b[np] = (uint8_t)(d - tlist[i] - 1);
+        ++np;
+      }
+      ++ng;
+    }
+  }
+  p.ngroups = ng;
+  p.group_begin[ng] = np;
+
+  int* sbuf = nullptr;
+  const size_t plane = (size_t)m * n;
+  if ((ce = cudaMallocAsync(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
+    return cuda_fail(ce, "Ozaki group sums");
+  p.sbuf = sbuf;
+  p.plane = (int64_t)plane;
+  p.status = ds->status;
+
+  auto kern = sp::slice_gemm_kernel<0, sp::EPI_OZAKI>;
+  ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
+  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+  const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
+  kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  note_launch();
+
+  cp.sbuf = sbuf;
+  cp.plane = (int64_t)plane;
+  cp.ngroups = ng;
+  cp.m = m;
+  cp.n = n;
+  cp.row_exp = rexp;
+  cp.col_exp = cexp;
+  cp.bits = bits;
+  cp.alpha = g.alpha;
+  cp.beta = g.beta;
+  cp.c = static_cast<double*>(g.c.ptr);
+  cp.rsc = g.c.rs;
+  cp.csc = g.c.cs;
+  const int64_t total = (int64_t)plane;
+  const int cblocks = (int)std::min<int64_t>(ceil_div(total, 256), (int64_t)ds->sm_count * 16);
+  combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+  note_launch();
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
+  cudaFreeAsync(planes_buf, s);
+  cudaFreeAsync(sbuf, s);
+  cudaFreeAsync(exps, s);
+  return MOMMS_OK;
+}
+
+}  // namespace momms

@@ -1,0 +1,96 @@
+// f32 GEMM as an error-compensated 3-term split-TF32 product on tcgen05.
+//
+// Each operand is split once into two TF32 planes, x = hi + lo with
+// hi = tf32_rna(x) and lo = tf32_rna(x - hi) (the subtraction is exact), and
+// C = beta*C + alpha*(A_lo B_hi + A_hi B_lo + A_hi B_hi) is accumulated in one
+// FP32 TMEM accumulator (the dropped A_lo B_lo term is below 2^-22 relative;
+// Markidis et al. 2018, Ootomo & Yokota 2022). The small cross terms are
+// accumulated first. The result stays inside the f32 componentwise bound
+// |dC| <= 2k u_32 (|A||B|) that the plain FFMA path meets.
+#include "internal.h"
+#include "planes.cuh"
+#include "slicegemm.cuh"
+
+namespace momms {
+
+namespace {
+struct Tf32SplitOp {
+  using Tout = float;
+  __device__ __forceinline__ void operator()(float v, int64_t, float* out, int64_t plane_elems) const {
+    uint32_t hi, lo;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(v));
+    const float rest = v - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(rest));
+    out[0] = __uint_as_float(hi);
+    out[plane_elems] = __uint_as_float(lo);
+  }
+};
+}  // namespace
+
+int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
+  DeviceState* ds = device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  const int64_t kp = round_up(g.k, 4);  // 16-byte rows for TMA
+  const size_t a_plane = (size_t)g.m * kp, b_plane = (size_t)g.n * kp;
+  void* buf = nullptr;
+  cudaError_t ce = cudaMallocAsync(&buf, (2 * a_plane + 2 * b_plane) * sizeof(float), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 planes");
+  float* pa = static_cast<float*>(buf);
+  float* pb = pa + 2 * a_plane;
+  planes::launch_to_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, (int64_t)a_plane,
+                           Tf32SplitOp{}, s);
+  planes::launch_to_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, (int64_t)b_plane,
+                           Tf32SplitOp{}, s);
+  note_launch(2);
+
+  CUtensorMap tmA, tmB;
+  {
+    uint64_t dims[3] = {(uint64_t)g.k, (uint64_t)g.m, 2};
+    uint64_t strides[2] = {(uint64_t)kp * 4, (uint64_t)a_plane * 4};
+    uint32_t box[3] = {32, (uint32_t)sp::BM, 1};
+    int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    uint64_t dimsb[3] = {(uint64_t)g.k, (uint64_t)g.n, 2};
+    uint64_t stridesb[2] = {(uint64_t)kp * 4, (uint64_t)b_plane * 4};
+    uint32_t boxb[3] = {32, (uint32_t)sp::BN, 1};
+    rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+  }
+
+  sp::Params p;
+  memset(&p, 0, sizeof(p));
+  p.m = g.m;
+  p.n = g.n;
+  p.kelems = 32;
+  p.kblocks = (int)ceil_div(g.k, 32);
+  p.tiles_m = (int)ceil_div(g.m, sp::BM);
+  p.tiles_n = (int)ceil_div(g.n, sp::BN);
+  p.ngroups = 1;
+  p.group_begin[0] = 0;
+  p.group_begin[1] = 3;
+  // small cross terms first, then hi*hi
+  p.pair_a[0] = 1; p.pair_b[0] = 0;  // A_lo * B_hi
+  p.pair_a[1] = 0; p.pair_b[1] = 1;  // A_hi * B_lo
+  p.pair_a[2] = 0; p.pair_b[2] = 0;  // A_hi * B_hi
+  p.chunk_kb[0] = 8;  // 256 k per tensor-core accumulation, then an RN add in registers
+  p.alpha_f = (float)g.alpha;
+  p.beta_f = (float)g.beta;
+  p.c32 = static_cast<float*>(g.c.ptr);
+  p.rsc = g.c.rs;
+  p.csc = g.c.cs;
+  p.status = ds->status;
+
+  auto kern = sp::slice_gemm_kernel<1, sp::EPI_F32>;
+  ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
+  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+  const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
+  kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  note_launch();
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 launch");
+  cudaFreeAsync(buf, s);
+  return MOMMS_OK;
+}
+
+}  // namespace momms

@@ -1,0 +1,289 @@
+// The slice-pair GEMM engine on tcgen05: C-tile accumulation of sums of
+// products of operand "planes" (precision slices of A and B) through TMEM.
+//
+//   for each output tile (persistent, one CTA per SM, 128 x 256 tiles):
+//     for each group g (processed in order):
+//       S_g = sum over pairs (a, b) in g of  A_plane[a] * B_plane[b]^T
+//       accumulated in TMEM in chunks of at most chunk_kb k-blocks; each
+//       finished chunk is handed to the epilogue (ping-pong TMEM buffers)
+//
+// Planes are K-major in HBM ([plane][row][k], k contiguous) and are loaded by
+// TMA as 128-byte-wide k-blocks with the 128B swizzle that the tcgen05 shared
+// memory descriptors expect. Warp roles: warp 0 issues TMA, warp 1 (one
+// thread) issues tcgen05.mma and commits, warps 2..9 drain TMEM.
+//
+// Two epilogues:
+//   EPI_F32   : one group; finished chunks are summed in FP32 registers
+//               (round to nearest) and C = alpha*sum + beta*C is written at
+//               the end of the tile. Used by the split-TF32 f32 path (pairs
+//               lo*hi, hi*lo, hi*hi).
+//   EPI_OZAKI : integer-valued slices; every chunk is exact in FP32 and is
+//               added into int32 accumulators; at the end of each group the
+//               exact sums are written to that group's int32 plane (the FP64
+//               recombination runs afterwards in its own kernel, so no FP64
+//               work sits in this pipeline).
+#pragma once
+#include <type_traits>
+
+#include "tc_common.cuh"
+
+namespace momms {
+namespace sp {
+
+constexpr int BM = 128, BN = 256, STAGES = 4;
+constexpr int A_TILE = BM * 128;  // bytes: 128 rows x 128-byte k-block
+constexpr int B_TILE = BN * 128;
+constexpr int STAGE_BYTES = A_TILE + B_TILE;  // 48 KB
+constexpr int EPI_WARPS = 8;                     // 2 per TMEM lane quarter
+constexpr int EPI_COLS = BN / (EPI_WARPS / 4);   // columns drained per thread
+constexpr int THREADS = (2 + EPI_WARPS) * 32;
+constexpr int TMEM_COLS = 512;  // two 128 x 256 f32 accumulators
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + 256;
+constexpr int MAX_GROUPS = 160, MAX_PAIRS = 160;
+
+enum { EPI_F32 = 0, EPI_OZAKI = 1 };
+
+struct Params {
+  int64_t m, n;
+  int kblocks;  // k-blocks per plane
+  int kelems;   // elements per k-block (64 for f16, 32 for tf32)
+  int tiles_m, tiles_n;
+  int ngroups;
+  int group_begin[MAX_GROUPS + 1];
+  int chunk_kb[MAX_GROUPS];
+  uint8_t pair_a[MAX_PAIRS], pair_b[MAX_PAIRS];
+  // EPI_F32
+  float alpha_f, beta_f;
+  float* c32;
+  // EPI_OZAKI: exact group sums, one column-major m x n int32 plane per group
+  int* sbuf;
+  int64_t plane;
+  int64_t rsc, csc;
+  unsigned* status;
+};
+
+__device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0; }
+
+// f32 integer value |x| <= 2^22 -> int32 via the 1.5*2^23 magic constant
+__device__ __forceinline__ int f2i_exact(uint32_t bits) {
+  const float f = __uint_as_float(bits) + 12582912.0f;
+  return (int)(__float_as_uint(f) - 0x4B400000u);
+}
+
+template <int KIND, int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const __grid_constant__ Params p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;  // [2]
+  uint64_t* tempty = tfull + 2;      // [2]
+  uint64_t* drain = tempty + 2;      // used only when aborting
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], EPI_WARPS);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+
+  if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
+    if (lane == 0) {
+      prefetch_tensormap(&tmA);
+      prefetch_tensormap(&tmB);
+      int stage = 0;
+      uint32_t ph = 0;
+      uint32_t armed = 0;  // bit s: stage s has been armed at least once
+      uint32_t last_ph = 0;  // bit s: parity of the phase last armed on stage s
+      for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+        const int tm = (int)(t % p.tiles_m), tn = (int)(t / p.tiles_m);
+        for (int g = 0; g < p.ngroups; ++g) {
+          for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
+            for (int kb = 0; kb < p.kblocks; ++kb) {
+              if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
+                report_status(p.status, DEV_TIMEOUT_EMPTY);
+                *abort_flag = 1;
+                // let every copy already issued land before the CTA exits
+                for (int s = 0; s < STAGES; ++s)
+                  if ((armed >> s) & 1u) mbar_wait_bounded(&full[s], (last_ph >> s) & 1u);
+                goto producer_done;
+              }
+              armed |= 1u << stage;
+              last_ph = (last_ph & ~(1u << stage)) | (ph << stage);
+              mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
+              uint8_t* sa = smem + stage * STAGE_BYTES;
+              tma_load_3d(sa, &tmA, &full[stage], kb * p.kelems, tm * BM, p.pair_a[pi]);
+              tma_load_3d(sa + A_TILE, &tmB, &full[stage], kb * p.kelems, tn * BN, p.pair_b[pi]);
+              if (++stage == STAGES) {
+                stage = 0;
+                ph ^= 1;
+              }
+            }
+          }
+        }
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    // ------------------------------ MMA issuer ------------------------------
+    if (lane == 0) {
+      const uint32_t idv = tc::idesc(KIND == 0 ? tc::FMT_F16 : tc::FMT_TF32, BM, BN);
+      int stage = 0;
+      uint32_t ph = 0;
+      int buf = 0;
+      uint32_t acc_ph[2] = {0, 0};
+      for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+        for (int g = 0; g < p.ngroups; ++g) {
+          const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
+          const int chunk = p.chunk_kb[g];
+          for (int s0 = 0; s0 < total; s0 += chunk) {
+            if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+              report_status(p.status, DEV_TIMEOUT_MMA);
+              *abort_flag = 1;
+              goto mma_done;
+            }
+            tc::fence_after();
+            const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+            const int s1 = min(total, s0 + chunk);
+            for (int st = s0; st < s1; ++st) {
+              if (!mbar_wait_bounded(&full[stage], ph)) {
+                report_status(p.status, DEV_TIMEOUT_FULL);
+                *abort_flag = 1;
+                goto mma_done;
+              }
+              tc::fence_after();
+              const uint32_t a_addr = smem_u32(smem + stage * STAGE_BYTES);
+              const uint32_t b_addr = a_addr + A_TILE;
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk)
+                tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
+                              (st > s0 || kk > 0) ? 1u : 0u);
+              tc::commit(&empty[stage]);
+              if (++stage == STAGES) {
+                stage = 0;
+                ph ^= 1;
+              }
+            }
+            tc::commit(&tfull[buf]);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
+          }
+        }
+      }
+    mma_done:
+      if (aborted(abort_flag)) {
+        // wait (bounded) until every MMA issued so far has completed, so that
+        // TMEM is not released under a running MMA
+        tc::commit(drain);
+        mbar_wait_bounded(drain, 0);
+      }
+    }
+  } else {
+    // ------------------------------ epilogue ------------------------------
+    const int q = warp & 3;              // TMEM lane quarter this warp may access
+    const int h = (warp - 2) >> 2;       // column group: cols h*EPI_COLS .. +EPI_COLS-1
+    const int r_local = q * 32 + lane;
+    int buf = 0;
+    uint32_t acc_ph[2] = {0, 0};
+    for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+      const int tm = (int)(t % p.tiles_m), tn = (int)(t / p.tiles_m);
+      const int64_t row = (int64_t)tm * BM + r_local;
+      const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
+      // per-thread accumulators of finished chunks: exact int32 digit sums
+      // (Ozaki) or FP32 sums rounded to nearest (split-TF32), which keeps the
+      // tensor core's internal accumulation to one chunk at a time
+      typedef typename std::conditional<EPI == EPI_OZAKI, int, float>::type Acc;
+      Acc S[EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+      for (int g = 0; g < p.ngroups; ++g) {
+        const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
+        const int chunk = p.chunk_kb[g];
+        for (int s0 = 0; s0 < total; s0 += chunk) {
+          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+            report_status(p.status, DEV_TIMEOUT_MMA);
+            *abort_flag = 1;
+            goto epi_done;
+          }
+          tc::fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+#pragma unroll
+          for (int pc = 0; pc < EPI_COLS / 16; ++pc) {
+            uint32_t r[16];
+            tc::ld16(taddr + pc * 16, r);
+            tc::ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              if (EPI == EPI_OZAKI) S[pc * 16 + j] += f2i_exact(r[j]);
+              else S[pc * 16 + j] += __uint_as_float(r[j]);
+            }
+          }
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[buf]);
+          acc_ph[buf] ^= 1;
+          buf ^= 1;
+        }
+        if (EPI == EPI_OZAKI) {
+          // end of group g: publish the exact int32 sums (column-major plane g)
+          if (row < p.m) {
+            int* srow = p.sbuf + (size_t)g * p.plane + row;
+#pragma unroll
+            for (int j = 0; j < EPI_COLS; ++j) {
+              const int64_t col = col0 + j;
+              if (col < p.n) srow[col * p.m] = (int)S[j];
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+        }
+      }
+      if (EPI == EPI_F32 && row < p.m) {
+        float* crow = p.c32 + row * p.rsc;
+#pragma unroll
+        for (int j = 0; j < EPI_COLS; ++j) {
+          const int64_t col = col0 + j;
+          if (col < p.n) {
+            float* cp = crow + col * p.csc;
+            const float v = (float)S[j] * p.alpha_f;
+            *cp = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, *cp, v);
+          }
+        }
+      }
+    }
+  epi_done:;
+  }
+
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem_base, TMEM_COLS);
+  }
+}
+
+}  // namespace sp
+}  // namespace momms
