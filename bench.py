@@ -1,19 +1,25 @@
 """Benchmark of the GB300 blocked matrix multiply (one JSON line on rank 0).
 
-Workload (the headline of the reference's shape sweep and the FP64 target):
-plain DGEMM C += A*B, m = n = k = 8192, column-major f64, entries uniform
-[-1, 1] from a fixed seed, alpha = beta = 1. Every operand (512 MiB) is larger
-than the 129 MB L2, so consecutive steps start cold without a flush.
+Workload: C += A*B with m = n = k = 8192, column-major f64, entries uniform
+[-1, 1] from a fixed seed, alpha = beta = 1 (the top of the reference-style
+square sweep and the FP64 target size). Every operand (512 MiB) is larger than
+the 129 MB L2, so consecutive steps start cold without a flush.
 
-  value : TFLOP/s = 2mnk / (device time per step), operands resident in HBM,
-          summed over ranks (replicas) and divided by the slowest rank's time.
-  e2e   : the same metric through momms_gemm() with pinned HOST operands:
-          each step copies A, B and C to the device and C back.
-  roofline : the DMMA kernel's achieved FP64 rate against the FP64 MMA peak
-          measured in this run (momms_measure_peak).
+The metric is FP64 GEMM throughput at FP64 accuracy, plain vs emulated:
+  value : TFLOP/s (2mnk / device time per step, operands resident in HBM) of
+          the emulated FP64 path (Ozaki slices on the fp16 tensor cores) at the
+          library's default FP64-level target, whose sampled componentwise
+          error is reported next to the plain path's in `accuracy`;
+  plain : the same problem on the FP64 tensor-core MMA (DMMA);
+  e2e   : the emulated path through momms_gemm() with pinned HOST operands
+          (H2D of A, B, C and D2H of C inside each timed step);
+  roofline : the dominant kernel (the tcgen05 slice-product kernel), its
+          fp16 tensor FLOP per launch over its CUDA-event duration, against
+          the measured bf16/fp16 dense peak; `plain.roofline` does the same for
+          the DMMA kernel against the FP64 peak measured in this run;
   cpu_baseline : the reference's Goto algorithm on the host cores (the
-          oracle's restatement; the reference's own asm kernels where they
-          can run), on a bounded sample of the same workload.
+          oracle's restatement; the reference's own asm kernels where they can
+          run), on a bounded sample of the same workload.
 
 --impl reference runs only that CPU algorithm, with every host thread, and
 prints its own line.
@@ -39,7 +45,7 @@ sys.path.insert(0, ROOT)
 METRIC = "FP64 GEMM TFLOP/s (plain vs emulated, equal error); served GEMM p50/p99 latency"
 SEED = 8192
 M = N = K = 8192
-WORKLOAD = "plain DGEMM C += A*B, m=n=k=8192, column-major f64, uniform[-1,1], alpha=beta=1"
+WORKLOAD = "DGEMM C += A*B, m=n=k=8192, column-major f64, uniform[-1,1], alpha=beta=1"
 
 
 def parse():
@@ -250,6 +256,55 @@ def profile_traffic(kernel_tag):
     return float(m.group(1)) if m else None
 
 
+def _desc(mg, m, n, k, a_ptr, b_ptr, c_ptr, mem, precision):
+    d = mg.GemmDesc()
+    d.dtype, d.precision = mg.DTYPE_F64, precision
+    d.m, d.n, d.k = m, n, k
+    d.alpha, d.beta = 1.0, 1.0
+    d.a = mg.Operand(a_ptr, 1, m, mem, 0)
+    d.b = mg.Operand(b_ptr, 1, k, mem, 0)
+    d.c = mg.Operand(c_ptr, 1, m, mem, 0)
+    d.target_rel_err = 0.0  # FP64 level
+    d.slices = 0            # chosen per call from the target
+    return d
+
+
+def _timed_steps(lib, mg, torch, stream, desc, dC, dC0, steps, warmup):
+    """Runs warmup + steps calls; returns (per-step event times in ms, kernel
+    launches of the library during the timed steps)."""
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            dC.copy_(dC0)
+            mg.check(lib.momms_gemm(ctypes.byref(desc), sp), lib)
+        stream.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        n0 = lib.momms_launch_count()
+        for i in range(steps):
+            dC.copy_(dC0)  # reset C (a device copy between the step's events)
+            ev[i][0].record(stream)
+            mg.check(lib.momms_gemm(ctypes.byref(desc), sp), lib)
+            ev[i][1].record(stream)
+        launches = lib.momms_launch_count() - n0
+        stream.synchronize()
+    return [a.elapsed_time(b) for a, b in ev], launches
+
+
+def _kernel_ms(lib, mg, cls):
+    tot = ctypes.c_double(0.0)
+    cnt = ctypes.c_ulonglong(0)
+    mg.check(lib.momms_timing_read(cls, ctypes.byref(tot), ctypes.byref(cnt), 1), lib)
+    return tot.value, cnt.value
+
+
+def _measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured (MEASURED_PEAKS.json)"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
 def run_ours(args):
     import torch
     import momms_gb300 as mg
@@ -264,74 +319,60 @@ def run_ours(args):
 
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
-    sp = ctypes.c_void_p(stream.cuda_stream)
     # device operands (column-major: a (cols, rows) tensor transposed)
     dA = torch.from_numpy(A.T.copy()).to(dev).t()
     dB = torch.from_numpy(B.T.copy()).to(dev).t()
     dC0 = torch.from_numpy(C0.T.copy()).to(dev).t()
     dC = torch.empty_like(dC0)
+    emu_desc = _desc(mg, m, n, k, dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), mg.MEM_DEVICE, mg.PREC_OZAKI)
+    plain_desc = _desc(mg, m, n, k, dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), mg.MEM_DEVICE, mg.PREC_PLAIN)
 
-    def desc(a_ptr, b_ptr, c_ptr, mem):
-        d = mg.GemmDesc()
-        d.dtype, d.precision = mg.DTYPE_F64, mg.PREC_PLAIN
-        d.m, d.n, d.k = m, n, k
-        d.alpha, d.beta = 1.0, 1.0
-        d.a = mg.Operand(a_ptr, 1, m, mem, 0)
-        d.b = mg.Operand(b_ptr, 1, k, mem, 0)
-        d.c = mg.Operand(c_ptr, 1, m, mem, 0)
-        return d
+    # ---- plain FP64 (DMMA): a few steps (about 1 s each at 8192) ----
+    lib.momms_timing_enable(1)
+    plain_steps = max(2, min(args.steps, 3))
+    plain_ms, _ = _timed_steps(lib, mg, torch, stream, plain_desc, dC, dC0, plain_steps, 1)
+    dmma_ms, dmma_n = _kernel_ms(lib, mg, mg.KERNEL_DGEMM_DMMA)
+    C_plain = dC.t().cpu().numpy().T
+    err_plain = sampled_error(A, B, C0, C_plain)
+    for cls in range(6):
+        _kernel_ms(lib, mg, cls)  # reset
 
-    dev_desc = desc(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), mg.MEM_DEVICE)
-
-    def step_device():
-        mg.check(lib.momms_gemm(ctypes.byref(dev_desc), sp), lib)
-
-    # C is reset from C0 before each step (a device copy, outside the per-step
-    # kernel timing below; the step time is taken from events around the GEMM)
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            dC.copy_(dC0)
-            step_device()
-        stream.synchronize()
-
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        launches0 = lib.momms_launch_count()
-        clocks = ClockSampler(local)
-        clocks.start()
-        barrier(world)
-        torch.cuda.synchronize()
-        t_start = time.perf_counter()
-        for i in range(args.steps):
-            dC.copy_(dC0)
-            ev[i][0].record(stream)
-            step_device()
-            ev[i][1].record(stream)
-        stream.synchronize()
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_start
-        clk = clocks.stop()
-        launches = lib.momms_launch_count() - launches0
-        step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    total_ms = max_over_ranks(total_ms, world)
+    # ---- emulated FP64: the timed region of the headline value ----
+    _timed_steps(lib, mg, torch, stream, emu_desc, dC, dC0, 0, args.warmup)
+    for cls in range(6):
+        _kernel_ms(lib, mg, cls)  # reset: count the timed steps only
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    t_start = time.perf_counter()
+    step_ms, launches = _timed_steps(lib, mg, torch, stream, emu_desc, dC, dC0, args.steps, 0)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_start
+    clk = clocks.stop()
+    info = mg.CallInfo()
+    lib.momms_last_info(ctypes.byref(info))
+    slice_ms, slice_n = _kernel_ms(lib, mg, mg.KERNEL_SLICE_OZAKI)
+    prep_ms, _ = _kernel_ms(lib, mg, mg.KERNEL_PREP)
+    comb_ms, _ = _kernel_ms(lib, mg, mg.KERNEL_COMBINE)
+    lib.momms_timing_enable(0)
+    total_ms = max_over_ranks(sum(step_ms), world)
     ms_per_step = total_ms / args.steps
     value = world * flops / (ms_per_step * 1e-3) / 1e12
-
-    # accuracy of the last result on a sample of entries
-    C_out = dC.t().cpu().numpy().T
-    acc_err = sampled_error(A, B, C0, C_out)
+    C_emu = dC.t().cpu().numpy().T
+    err_emu = sampled_error(A, B, C0, C_emu)
 
     # ---- e2e through the public API with pinned host operands ----
     hA = torch.from_numpy(A.T.copy()).pin_memory().t()
     hB = torch.from_numpy(B.T.copy()).pin_memory().t()
     hC0 = torch.from_numpy(C0.T.copy()).pin_memory().t()
     hC = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
-    host_desc = desc(hA.data_ptr(), hB.data_ptr(), hC.data_ptr(), mg.MEM_HOST)
-    e2e_steps = max(3, args.steps // 2)
-    for _ in range(1):
-        hC.copy_(hC0)
-        mg.check(lib.momms_gemm(ctypes.byref(host_desc), sp), lib)
+    host_desc = _desc(mg, m, n, k, hA.data_ptr(), hB.data_ptr(), hC.data_ptr(), mg.MEM_HOST, mg.PREC_OZAKI)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    hC.copy_(hC0)
+    mg.check(lib.momms_gemm(ctypes.byref(host_desc), sp), lib)
     barrier(world)
+    e2e_steps = max(3, args.steps)
     e2e_t = 0.0
     for _ in range(e2e_steps):
         hC.copy_(hC0)  # host-side reset, not timed
@@ -340,16 +381,19 @@ def run_ours(args):
         e2e_t += time.perf_counter() - t0
     e2e_t = max_over_ranks(e2e_t, world)
     e2e_value = world * flops * e2e_steps / e2e_t / 1e12
-    elem = 8
-    h2d = 3 * m * k * elem  # A, B and C (beta = 1 reads C)
-    d2h = m * n * elem
+    h2d = 3 * m * k * 8  # A, B and C (beta = 1 reads C)
+    d2h = m * n * 8
 
-    # ---- roofline: achieved FP64 MMA rate vs the measured peak ----
-    peak = ctypes.c_double(0.0)
-    mg.check(lib.momms_measure_peak(0, ctypes.byref(peak)), lib)
-    kernel_ms = statistics.mean(step_ms)
-    achieved = flops / (kernel_ms * 1e-3) / 1e12
-    traffic = profile_traffic("dgemm_dmma_8192")
+    # ---- rooflines ----
+    peaks, peak_src = _measured_peaks()
+    tc_flops_per_launch = info.pairs * flops  # fp16 MMA work of the slice kernel
+    slice_avg = slice_ms / max(1, slice_n)
+    tc_achieved = tc_flops_per_launch / (slice_avg * 1e-3) / 1e12
+    tc_peak = float(peaks["bf16_tflops"])
+    fp64_peak = ctypes.c_double(0.0)
+    mg.check(lib.momms_measure_peak(0, ctypes.byref(fp64_peak)), lib)
+    dmma_avg = dmma_ms / max(1, dmma_n)
+    dmma_achieved = flops / (dmma_avg * 1e-3) / 1e12
 
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -357,17 +401,33 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64",
         "data": f"synthetic: uniform[-1,1] from seed {SEED}, column-major, C initialised like A and B",
         "config": {"workload": WORKLOAD.replace("8192", str(size)), "m": m, "n": n, "k": k,
-                   "precision": "plain (FP64 tensor-core MMA, mma.sync m8n8k4)",
+                   "precision": "emulated FP64 (Ozaki: 7-bit fp16 digit slices on tcgen05, exact int32 "
+                                "digit sums, FP64 recombination); slice count chosen per call for the "
+                                "default FP64-level target",
+                   "slices": info.slices, "slice_products": info.pairs,
                    "l2": "inputs larger than L2 (512 MiB per operand vs 129 MB L2); no flush",
                    "parallelism": f"replicas x{world}"},
-        "accuracy": {"max_rel_err_sampled": acc_err, "definition": "max |C-exact|/(|A||B|+|C0|) over 128 entries"},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
-                     "peak_source": "FP64 DMMA issue rate measured in this run (momms_measure_peak kind 0); "
-                                    "not in MEASURED_PEAKS.json, which has HBM and bf16 only",
-                     "kernel": "momms::dmma::dgemm_kernel", "algorithmic_flops_per_launch": flops},
+        "accuracy": {"max_rel_err_emulated": err_emu, "max_rel_err_plain": err_plain,
+                     "emulated_bound_rel_err": info.bound_rel_err,
+                     "definition": "max |C-exact|/(|A||B|+|C0|) over the same 128 sampled entries; exact "
+                                   "by error-free products and math.fsum"},
+        "plain": {"value": flops / (statistics.mean(plain_ms) * 1e-3) / 1e12, "unit": "TFLOP/s",
+                  "ms_per_step": statistics.mean(plain_ms), "steps": plain_steps,
+                  "roofline": {"bound": "tensor", "achieved": dmma_achieved, "peak": fp64_peak.value,
+                               "unit": "TFLOP/s", "frac": dmma_achieved / fp64_peak.value if fp64_peak.value else None,
+                               "traffic": profile_traffic("dgemm_dmma_8192"),
+                               "peak_source": "FP64 DMMA issue rate measured in this run (momms_measure_peak)",
+                               "kernel": "momms::dmma::dgemm_kernel"}},
+        "speedup_emulated_vs_plain": value / (flops / (statistics.mean(plain_ms) * 1e-3) / 1e12),
+        "roofline": {"bound": "tensor", "achieved": tc_achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                     "frac": tc_achieved / tc_peak, "traffic": profile_traffic("slice_gemm_ozaki_8192"),
+                     "peak_source": f"bf16 dense cuBLAS burst, {peak_src} (fp16 and bf16 share the tcgen05 rate)",
+                     "kernel": "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>",
+                     "algorithmic_flops_per_launch": tc_flops_per_launch,
+                     "kernel_ms_per_launch": slice_avg,
+                     "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps}},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps, "api": "momms_gemm with MOMMS_MEM_HOST pinned operands"},
+                "steps": e2e_steps, "api": "momms_gemm, MOMMS_PREC_OZAKI, MOMMS_MEM_HOST pinned operands"},
         "gpu_launches": int(launches),
         "clocks": clk,
         "wall_s_timed": t_wall,

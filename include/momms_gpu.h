@@ -129,6 +129,19 @@ int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, co
                         int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
                         int64_t rs_c, int64_t cs_c, void* stream);
 
+/* What the calling thread's last successful momms_gemm did. No reference
+ * counterpart (the reference's blocking is fixed at compile time). */
+typedef struct {
+  int32_t precision;      /* momms_precision actually run */
+  int32_t slices;         /* OZAKI: slice count used (chosen or given) */
+  int32_t pairs;          /* OZAKI: slice products formed (tensor-core GEMMs) */
+  int32_t groups;         /* OZAKI: accumulation groups */
+  int32_t splits;         /* plain paths: k splits */
+  int32_t reserved;
+  double bound_rel_err;   /* OZAKI: predicted worst-case |dC|/(|A||B|) */
+} momms_call_info;
+int momms_last_info(momms_call_info* out);
+
 /* Checks a descriptor without touching the GPU: sizes, strides, enums.
  * Returns MOMMS_OK or MOMMS_ERR_INVALID_ARG / MOMMS_ERR_UNSUPPORTED. */
 int momms_gemm_validate(const momms_gemm_desc* desc);
@@ -149,6 +162,23 @@ int momms_abi_version(void);
 /* Number of kernels this library has launched in this process (all devices).
  * No reference counterpart: evidence for benchmarks of what ran on the GPU. */
 unsigned long long momms_launch_count(void);
+
+/* Per-kernel timing, off by default. While on, every launch of the library's
+ * kernels is bracketed by CUDA events on its launching stream and the elapsed
+ * time is accumulated per kernel class (no host synchronisation on the launch
+ * path; momms_timing_read synchronises the recorded events). No reference
+ * counterpart (the reference times whole runs, src/util.rs:87-92). */
+typedef enum {
+  MOMMS_KERNEL_DGEMM_DMMA = 0,   /* plain f64 */
+  MOMMS_KERNEL_SGEMM_FFMA = 1,   /* plain f32 */
+  MOMMS_KERNEL_SLICE_OZAKI = 2,  /* tcgen05 slice products, Ozaki f64 */
+  MOMMS_KERNEL_SLICE_TF32 = 3,   /* tcgen05 slice products, split-TF32 f32 */
+  MOMMS_KERNEL_PREP = 4,         /* exponent scan, slicing / splitting, repack */
+  MOMMS_KERNEL_COMBINE = 5,      /* Ozaki FP64 recombination */
+  MOMMS_KERNEL_CLASSES = 6
+} momms_kernel_class;
+int momms_timing_enable(int on);
+int momms_timing_read(int kernel_class, double* total_ms, unsigned long long* launches, int reset);
 
 /* Measures the current device's peak issue rate in TFLOP/s with a
  * register-only loop: kind 0 = FP64 tensor-core MMA (DMMA m8n8k4),

@@ -25,6 +25,13 @@ ERR_ADMISSION = 7
 ERR_BUSY = 8
 ERR_SHUTDOWN = 9
 
+KERNEL_DGEMM_DMMA = 0
+KERNEL_SGEMM_FFMA = 1
+KERNEL_SLICE_OZAKI = 2
+KERNEL_SLICE_TF32 = 3
+KERNEL_PREP = 4
+KERNEL_COMBINE = 5
+
 DTYPE_F64 = 0
 DTYPE_F32 = 1
 PREC_PLAIN = 0
@@ -47,6 +54,12 @@ class GemmDesc(ctypes.Structure):
                 ("a", Operand), ("b", Operand), ("c", Operand),
                 ("target_rel_err", ctypes.c_double), ("slices", ctypes.c_int32),
                 ("flags", ctypes.c_int32)]
+
+
+class CallInfo(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("slices", ctypes.c_int32), ("pairs", ctypes.c_int32),
+                ("groups", ctypes.c_int32), ("splits", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("bound_rel_err", ctypes.c_double)]
 
 
 class MommsError(RuntimeError):
@@ -93,6 +106,12 @@ def load_library(path=None):
     lib.momms_launch_count.restype = ctypes.c_ulonglong
     lib.momms_measure_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     lib.momms_measure_peak.restype = i32
+    lib.momms_last_info.argtypes = [ctypes.POINTER(CallInfo)]
+    lib.momms_last_info.restype = i32
+    lib.momms_timing_enable.argtypes = [i32]
+    lib.momms_timing_enable.restype = i32
+    lib.momms_timing_read.argtypes = [i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_ulonglong), i32]
+    lib.momms_timing_read.restype = i32
     if path is None:
         _lib = lib
     return lib

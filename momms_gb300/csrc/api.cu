@@ -14,9 +14,13 @@ namespace momms {
 
 namespace {
 thread_local char g_last_error[512] = "";
+thread_local momms_call_info g_info;
+thread_local momms_call_info g_last_info;
 std::mutex g_dev_mu;
 DeviceState g_devices[64];
 }  // namespace
+
+momms_call_info& call_info() { return g_info; }
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -112,6 +116,7 @@ int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, 
   if (total == 0) return MOMMS_OK;
   const int threads = 256;
   const int blocks = (int)std::min<int64_t>(ceil_div(total, threads), 4096);
+  KernelTimer kt(MOMMS_KERNEL_PREP, s);
   if (elem == 8)
     repack_kernel<double><<<blocks, threads, 0, s>>>(static_cast<const double*>(src.ptr), src.rs, src.cs, rows, cols,
                                                       static_cast<double*>(dst), ld);
@@ -271,6 +276,9 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   // is (src/composables/part.rs:98-106); so does this node.
   if (d->m == 0 || d->n == 0 || d->k == 0) return MOMMS_OK;
   if (!device_state()) return MOMMS_ERR_NO_DEVICE;
+  memset(&g_info, 0, sizeof(g_info));
+  g_info.precision = d->precision;
+  g_info.bound_rel_err = -1.0;
   const size_t es = elem_size(d->dtype);
   const momms_operand* ops[3] = {&d->a, &d->b, &d->c};
   const int64_t rows[3] = {d->m, d->k, d->m}, cols[3] = {d->k, d->n, d->n};
@@ -304,6 +312,7 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (!rc && e != cudaSuccess) rc = cuda_fail(e, "stream synchronize");
   }
+  if (!rc) g_last_info = g_info;
   return rc;
 }
 
@@ -390,5 +399,11 @@ const char* momms_status_string(int status) {
 const char* momms_last_error(void) { return momms::g_last_error; }
 
 int momms_abi_version(void) { return MOMMS_ABI_VERSION; }
+
+int momms_last_info(momms_call_info* out) {
+  if (!out) return momms::fail(MOMMS_ERR_INVALID_ARG, "out is null");
+  *out = momms::g_last_info;
+  return MOMMS_OK;
+}
 
 }  // extern "C"

@@ -17,6 +17,7 @@ enum : unsigned {
   DEV_TIMEOUT_EMPTY = 2u,  // producer gave up waiting for a free stage
   DEV_TIMEOUT_MMA = 4u,    // epilogue gave up waiting for the tensor core
   DEV_BAD_CONFIG = 8u,     // launch shape does not match the kernel
+  DEV_TIMEOUT_TMEM = 16u,  // MMA issuer gave up waiting for a drained accumulator
 };
 
 // Upper bound on polls of one mbarrier wait. A healthy pipeline completes a

@@ -350,6 +350,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);
   p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};
+  call_info().splits = splits;
   p.partials = nullptr;
   p.counters = nullptr;
   void* ws = nullptr;
@@ -367,7 +368,10 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   auto launch = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    kern<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+    {
+      KernelTimer kt(MOMMS_KERNEL_DGEMM_DMMA, s);
+      kern<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+    }
     note_launch();
     return cudaGetLastError();
   };

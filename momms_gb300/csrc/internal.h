@@ -60,8 +60,26 @@ int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int*
 int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, void* dst, int64_t ld,
                     cudaStream_t s);
 
+// Record of the calling thread's current / last momms_gemm call.
+momms_call_info& call_info();
+
 // Counts kernel launches made by this library (momms_launch_count()).
 void note_launch(int n = 1);
+
+// Brackets the launches made during its lifetime with CUDA events on `s`
+// when momms_timing_enable(1) is in effect (see momms_timing_read).
+class KernelTimer {
+ public:
+  KernelTimer(int cls, cudaStream_t s);
+  ~KernelTimer();
+  KernelTimer(const KernelTimer&) = delete;
+  KernelTimer& operator=(const KernelTimer&) = delete;
+
+ private:
+  int cls_;
+  cudaStream_t s_;
+  cudaEvent_t a_, b_;
+};
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }

@@ -36,60 +36,94 @@ namespace {
 
 constexpr int kDigitBits = 7;
 
-// Exponent e with max_p |x(r,p)| < 2^e (frexp); 0 for an all-zero row;
-// INT32_MAX when the row holds a NaN or an infinity.
-__global__ void __launch_bounds__(256) row_exp_kernel(const double* __restrict__ x, int64_t sr, int64_t sp, int64_t R,
-                                                      int64_t K, bool r_contig, int* __restrict__ exps) {
-  __shared__ double red[8][33];
-  __shared__ int bad[8][33];
+// Everything in the pre-pass runs on integer bit patterns: GB300's FP64 pipe
+// is about 1 TFLOP/s, so FP64 arithmetic per element would dominate.
+
+// |v| as an unsigned bit pattern: for non-negative doubles the unsigned order
+// of the patterns is the order of the values; infinities and NaNs sort above
+// every finite value.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+// Row maxima of |x(r, p)| as bit patterns. A block covers 32 rows x 256 of p,
+// reads along whichever index is contiguous, reduces in registers / shared
+// memory and posts one atomicMax per row (maxbits must start at zero).
+__global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
+                                                         int64_t R, int64_t K, bool r_contig,
+                                                         unsigned long long* __restrict__ maxbits) {
+  __shared__ unsigned long long red[8][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 256;
   if (r_contig) {
-    // threads along r (the contiguous index), ty strides over p
+    // lanes along r, ty strides over p
     const int64_t r = r0 + tx;
-    double mx = 0.0;
-    int nf = 0;
+    unsigned long long mx = 0;
     if (r < R)
-      for (int64_t pp = ty; pp < K; pp += 8) {
-        const double v = x[r * sr + pp * sp];
-        nf |= !isfinite(v);
-        mx = fmax(mx, fabs(v));
+      for (int j = 0; j < 32; ++j) {
+        const int64_t pp = p0 + ty + 8 * j;
+        if (pp < K) mx = max(mx, abs_bits(x[r * sr + pp * sp]));
       }
     red[ty][tx] = mx;
-    bad[ty][tx] = nf;
     __syncthreads();
     if (ty == 0 && r < R) {
-      for (int i = 1; i < 8; ++i) {
-        mx = fmax(mx, red[i][tx]);
-        nf |= bad[i][tx];
-      }
-      int e = 0;
-      if (!nf && mx > 0.0) frexp(mx, &e);
-      exps[r] = nf ? INT32_MAX : e;
+      for (int i = 1; i < 8; ++i) mx = max(mx, red[i][tx]);
+      if (mx) atomicMax(&maxbits[r], mx);
     }
   } else {
     // one warp per row, lanes along p
     for (int i = 0; i < 4; ++i) {
       const int64_t r = r0 + ty + 8 * i;
       if (r >= R) break;
-      double mx = 0.0;
-      int nf = 0;
-      for (int64_t pp = tx; pp < K; pp += 32) {
-        const double v = x[r * sr + pp * sp];
-        nf |= !isfinite(v);
-        mx = fmax(mx, fabs(v));
+      unsigned long long mx = 0;
+      for (int j = 0; j < 8; ++j) {
+        const int64_t pp = p0 + tx + 32 * j;
+        if (pp < K) mx = max(mx, abs_bits(x[r * sr + pp * sp]));
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        nf |= __shfl_xor_sync(0xffffffffu, nf, o);
-      }
-      if (tx == 0) {
-        int e = 0;
-        if (!nf && mx > 0.0) frexp(mx, &e);
-        exps[r] = nf ? INT32_MAX : e;
-      }
+      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (tx == 0 && mx) atomicMax(&maxbits[r], mx);
     }
   }
+}
+
+// Exponent e with max |x| < 2^e (the frexp exponent of the maximum); 0 for an
+// all-zero row; INT32_MAX for a row holding a NaN or an infinity.
+__global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int64_t count, int* __restrict__ exps) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const unsigned long long b = maxbits[i];
+  int e;
+  if (b >= 0x7ff0000000000000ull) e = INT32_MAX;
+  else if (b == 0) e = 0;
+  else if ((b >> 52) != 0) e = (int)(b >> 52) - 1022;  // [2^(be-1023), 2^(be-1022))
+  else e = (63 - __clzll((long long)b)) - 1073;         // subnormal
+  exps[i] = e;
+}
+
+// Signed digits of v * 2^-e at `bits` bits each, nearest rounding at the last
+// digit: X = round(|v| * 2^(bits*slices - e)) as an integer, then centred
+// digits are peeled from the bottom (each in [-2^(bits-1), 2^(bits-1))) and the
+// remaining top digit lies in [0, 2^bits]. Returns the digits of |v|; the
+// caller applies the sign. U is uint64 (bits*slices <= 62) or __int128.
+template <typename U>
+__device__ __forceinline__ void digits_of(unsigned long long ab, int e, int bits, int slices, int* d) {
+  const unsigned long long frac = ab & ((1ull << 52) - 1);
+  const int be = (int)(ab >> 52);
+  const unsigned long long M = be ? (frac | (1ull << 52)) : frac;
+  const int E = be ? be - 1075 : -1074;  // |v| = M * 2^E
+  const int sh = E - e + bits * slices;
+  U X;
+  if (sh >= 0) X = (U)M << sh;
+  else if (sh > -64) X = (U)((M >> (-sh)) + ((M >> (-sh - 1)) & 1ull));
+  else X = 0;
+  const U mask = ((U)1 << bits) - 1, half = (U)1 << (bits - 1);
+  for (int t = slices - 1; t >= 1; --t) {
+    const U low = X & mask;
+    const int dt = (low >= half) ? (int)low - (1 << bits) : (int)low;
+    d[t] = dt;
+    X = (dt < 0) ? ((X + (U)(-dt)) >> bits) : ((X - (U)dt) >> bits);
+  }
+  d[0] = (int)X;
 }
 
 struct OzakiSliceOp {
@@ -99,14 +133,17 @@ struct OzakiSliceOp {
   int bits;
   __device__ __forceinline__ void operator()(double v, int64_t r, __half* out, int64_t plane_elems) const {
     const int e = exps[r];
-    double x = (e == INT32_MAX) ? 0.0 : ldexp(v, -e);
-    const double up = (double)(1 << bits);
-    for (int t = 0; t < slices; ++t) {
-      const double y = x * up;  // exact (power of two)
-      const double d = rint(y);
-      x = y - d;  // exact: |y - rint(y)| <= 1/2
-      out[(int64_t)t * plane_elems] = __double2half(d);
+    int d[16];
+    const unsigned long long ab = abs_bits(v);
+    if (e == INT32_MAX || ab == 0) {
+      for (int t = 0; t < slices; ++t) d[t] = 0;
+    } else if (bits * slices <= 62) {
+      digits_of<unsigned long long>(ab, e, bits, slices, d);
+    } else {
+      digits_of<unsigned __int128>(ab, e, bits, slices, d);
     }
+    const bool neg = __double_as_longlong(v) < 0;
+    for (int t = 0; t < slices; ++t) out[(int64_t)t * plane_elems] = __int2half_rn(neg ? -d[t] : d[t]);
   }
 };
 
@@ -200,9 +237,12 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int64_t m = g.m, n = g.n, k = g.k;
   cudaError_t ce;
 
-  int* exps = nullptr;
-  if ((ce = cudaMallocAsync(&exps, (size_t)(m + n) * sizeof(int), s)) != cudaSuccess)
+  // exponents: [m + n] u64 maxima followed by [m + n] int exponents
+  void* ebuf = nullptr;
+  if ((ce = cudaMallocAsync(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki exponents");
+  unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
+  int* exps = reinterpret_cast<int*>(maxbits + (m + n));
   int* rexp = exps;
   int* cexp = exps + m;
   const double* A = static_cast<const double*>(g.a.ptr);
@@ -210,9 +250,16 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   {
     // A viewed as m x k; B viewed transposed, n x k
     const bool a_rc = (g.a.rs == 1 && g.a.cs != 1), b_rc = (g.b.cs == 1 && g.b.rs != 1);
-    row_exp_kernel<<<(unsigned)ceil_div(m, 32), dim3(32, 8), 0, s>>>(A, g.a.rs, g.a.cs, m, k, a_rc, rexp);
-    row_exp_kernel<<<(unsigned)ceil_div(n, 32), dim3(32, 8), 0, s>>>(B, g.b.cs, g.b.rs, n, k, b_rc, cexp);
-    note_launch(2);
+    KernelTimer kt(MOMMS_KERNEL_PREP, s);
+    if ((ce = cudaMemsetAsync(maxbits, 0, (size_t)(m + n) * sizeof(unsigned long long), s)) != cudaSuccess)
+      return cuda_fail(ce, "Ozaki exponents");
+    const dim3 blk(32, 8);
+    row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(m, 32)), blk, 0, s>>>(
+        A, g.a.rs, g.a.cs, m, k, a_rc, maxbits);
+    row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(n, 32)), blk, 0, s>>>(
+        B, g.b.cs, g.b.rs, n, k, b_rc, maxbits + m);
+    exps_kernel<<<(unsigned)ceil_div(m + n, 256), 256, 0, s>>>(maxbits, m + n, exps);
+    note_launch(3);
   }
 
   int ns = slices;
@@ -239,6 +286,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     if (!(q2 > 0.0)) q2 = 4.0;
     ns = 1;
     while (ns < 16 && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
+    call_info().bound_rel_err = ozaki_bound(ns, bits, q1, q2);
   }
   if (slices_used) *slices_used = ns;
 
@@ -249,8 +297,11 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     return cuda_fail(ce, "Ozaki slice planes");
   __half* pa = planes_buf;
   __half* pb = planes_buf + (size_t)ns * a_plane;
-  planes::launch_to_planes(A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, OzakiSliceOp{rexp, ns, bits}, s);
-  planes::launch_to_planes(B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, OzakiSliceOp{cexp, ns, bits}, s);
+  {
+    KernelTimer kt(MOMMS_KERNEL_PREP, s);
+    planes::launch_to_planes(A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, OzakiSliceOp{rexp, ns, bits}, s);
+    planes::launch_to_planes(B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, OzakiSliceOp{cexp, ns, bits}, s);
+  }
   note_launch(2);
 
   if (k > 65536) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 (int32 digit sums)");
@@ -314,6 +365,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   }
   p.ngroups = ng;
   p.group_begin[ng] = np;
+  call_info().slices = ns;
+  call_info().pairs = np;
+  call_info().groups = ng;
 
   int* sbuf = nullptr;
   const size_t plane = (size_t)m * n;
@@ -328,7 +382,10 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
   const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
-  kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  {
+    KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, s);
+    kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  }
   note_launch();
 
   cp.sbuf = sbuf;
@@ -346,13 +403,16 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.csc = g.c.cs;
   const int64_t total = (int64_t)plane;
   const int cblocks = (int)std::min<int64_t>(ceil_div(total, 256), (int64_t)ds->sm_count * 16);
-  combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+  {
+    KernelTimer kt(MOMMS_KERNEL_COMBINE, s);
+    combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+  }
   note_launch();
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
   cudaFreeAsync(planes_buf, s);
   cudaFreeAsync(sbuf, s);
-  cudaFreeAsync(exps, s);
+  cudaFreeAsync(ebuf, s);
   return MOMMS_OK;
 }
 

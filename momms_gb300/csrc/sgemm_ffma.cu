@@ -243,6 +243,7 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);
   p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};
+  call_info().splits = splits;
   p.partials = nullptr;
   p.counters = nullptr;
   void* ws = nullptr;
@@ -255,18 +256,21 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
     if ((ce = cudaMemsetAsync(p.counters, 0, cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "memset counters");
   }
   const int grid = (int)std::min<int64_t>(p.sched.units(), slots);
-  if (a_xc && b_xc) {
-    if (vec) sgemm_kernel<true, true, true><<<grid, THREADS, 0, s>>>(p);
-    else sgemm_kernel<true, true, false><<<grid, THREADS, 0, s>>>(p);
-  } else if (a_xc) {
-    if (vec) sgemm_kernel<true, false, true><<<grid, THREADS, 0, s>>>(p);
-    else sgemm_kernel<true, false, false><<<grid, THREADS, 0, s>>>(p);
-  } else if (b_xc) {
-    if (vec) sgemm_kernel<false, true, true><<<grid, THREADS, 0, s>>>(p);
-    else sgemm_kernel<false, true, false><<<grid, THREADS, 0, s>>>(p);
-  } else {
-    if (vec) sgemm_kernel<false, false, true><<<grid, THREADS, 0, s>>>(p);
-    else sgemm_kernel<false, false, false><<<grid, THREADS, 0, s>>>(p);
+  {
+    KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
+    if (a_xc && b_xc) {
+      if (vec) sgemm_kernel<true, true, true><<<grid, THREADS, 0, s>>>(p);
+      else sgemm_kernel<true, true, false><<<grid, THREADS, 0, s>>>(p);
+    } else if (a_xc) {
+      if (vec) sgemm_kernel<true, false, true><<<grid, THREADS, 0, s>>>(p);
+      else sgemm_kernel<true, false, false><<<grid, THREADS, 0, s>>>(p);
+    } else if (b_xc) {
+      if (vec) sgemm_kernel<false, true, true><<<grid, THREADS, 0, s>>>(p);
+      else sgemm_kernel<false, true, false><<<grid, THREADS, 0, s>>>(p);
+    } else {
+      if (vec) sgemm_kernel<false, false, true><<<grid, THREADS, 0, s>>>(p);
+      else sgemm_kernel<false, false, false><<<grid, THREADS, 0, s>>>(p);
+    }
   }
   note_launch();
   ce = cudaGetLastError();

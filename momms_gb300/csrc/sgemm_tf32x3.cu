@@ -37,10 +37,13 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 planes");
   float* pa = static_cast<float*>(buf);
   float* pb = pa + 2 * a_plane;
-  planes::launch_to_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, (int64_t)a_plane,
-                           Tf32SplitOp{}, s);
-  planes::launch_to_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, (int64_t)b_plane,
-                           Tf32SplitOp{}, s);
+  {
+    KernelTimer kt(MOMMS_KERNEL_PREP, s);
+    planes::launch_to_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, (int64_t)a_plane,
+                             Tf32SplitOp{}, s);
+    planes::launch_to_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, (int64_t)b_plane,
+                             Tf32SplitOp{}, s);
+  }
   note_launch(2);
 
   CUtensorMap tmA, tmB;
@@ -85,7 +88,10 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
   const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
-  kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  {
+    KernelTimer kt(MOMMS_KERNEL_SLICE_TF32, s);
+    kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+  }
   note_launch();
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 launch");

@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           const int chunk = p.chunk_kb[g];
           for (int s0 = 0; s0 < total; s0 += chunk) {
             if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-              report_status(p.status, DEV_TIMEOUT_MMA);
+              report_status(p.status, DEV_TIMEOUT_TMEM);
               *abort_flag = 1;
               goto mma_done;
             }
@@ -277,6 +277,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   epi_done:;
   }
 
+  // reconverge each warp (its lane 0 may have run a role loop alone) before
+  // the CTA-wide barrier, which requires whole warps
+  __syncwarp();
   tc::fence_before();
   __syncthreads();
   if (warp == 1) {

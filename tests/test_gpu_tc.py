@@ -165,3 +165,17 @@ def test_ozaki_deterministic(gpu):
     C1 = gu.gemm_device(gpu, A, B, C0, precision=mg.PREC_OZAKI)
     C2 = gu.gemm_device(gpu, A, B, C0, precision=mg.PREC_OZAKI)
     assert np.array_equal(C1, C2)
+
+
+def test_no_bounded_wait_expired(gpu):
+    """No kernel of the tcgen05 paths gave up on a barrier during this module."""
+    import ctypes
+    rng = np.random.default_rng(12)
+    A, B, C0 = _mats(rng, 1000, 1000, 2000, np.float64)
+    gu.gemm_device(gpu, A, B, C0, precision=mg.PREC_OZAKI)
+    A32, B32, C32 = (x.astype(np.float32) for x in (A, B, C0))
+    gu.gemm_device(gpu, np.asfortranarray(A32), np.asfortranarray(B32), np.asfortranarray(C32),
+                   precision=mg.PREC_SPLIT_TF32)
+    bits = ctypes.c_uint32(0)
+    assert gpu.momms_device_status(ctypes.byref(bits)) == mg.OK, bits.value
+    assert bits.value == 0
