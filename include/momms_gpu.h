@@ -32,6 +32,7 @@
 #ifndef MOMMS_GPU_H
 #define MOMMS_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -128,6 +129,51 @@ int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float
 int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a,
                         int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
                         int64_t rs_c, int64_t cs_c, void* stream);
+
+/* ---- Grouped launches and execution plans --------------------------------
+ * Many independent GEMMs run as one persistent kernel per dtype: every plain
+ * f64 problem's tiles (and k-splits) are work units of one DMMA kernel, every
+ * plain f32 problem's of one FFMA kernel; Ozaki and split-TF32 problems run
+ * their own kernel sequences after them. Each problem is planned from its own
+ * shape only (tile, split-k: the tuning table or the model), so a problem
+ * gives bit-identical results alone (momms_gemm) and in any batch. Plans take
+ * device operands only. The reference runs one composed algorithm per call
+ * (src/exper/l3.rs:46-93); it has no batched form. */
+typedef struct momms_plan_s* momms_plan;
+
+/* Builds the problem tables, tensor maps and split-k workspaces once
+ * (synchronous). Operand pointers are captured: later launches read the
+ * current contents of the same buffers. An Ozaki problem with slices == 0 has
+ * its slice count chosen here from the operands' current contents. */
+int momms_plan_create(const momms_gemm_desc* descs, int count, momms_plan* out);
+/* Enqueues the plan on `stream` (its CUDA graph if captured). Asynchronous;
+ * launches of one plan must not overlap each other on the GPU (they share
+ * the plan's workspaces). */
+int momms_plan_launch(momms_plan plan, void* stream);
+/* Captures the plan's launches into a CUDA graph owned by the plan; later
+ * momms_plan_launch calls launch the graph (one launch for the whole batch). */
+int momms_plan_capture(momms_plan plan, void* stream);
+int momms_plan_destroy(momms_plan plan);
+/* Convenience: create, launch, synchronise `stream`, destroy. */
+int momms_gemm_grouped(const momms_gemm_desc* descs, int count, void* stream);
+
+/* ---- Autotuning -----------------------------------------------------------
+ * The runtime analogue of the reference's compile-time block sizes
+ * (typenum NC/KC/MC/MR/NR, src/exper/l3_packing.rs:58-66): times the split-k
+ * candidates of a plain problem on its device operands (writing only a scratch
+ * C) and records the fastest in a process-wide table keyed by
+ * (dtype, precision, m, n, k) that momms_gemm and plans consult. Synchronous. */
+typedef struct {
+  int32_t splits;     /* chosen k-split count */
+  int32_t candidates; /* configurations timed */
+  float best_ms;      /* time of the chosen configuration */
+  int32_t reserved;
+} momms_tune_result;
+int momms_autotune(const momms_gemm_desc* desc, momms_tune_result* out, void* stream);
+/* Table as text, one "dtype precision m n k splits" line per entry. */
+int momms_tune_export(char* buf, size_t cap, size_t* needed);
+int momms_tune_import(const char* text);
+int momms_tune_clear(void);
 
 /* What the calling thread's last successful momms_gemm did. No reference
  * counterpart (the reference's blocking is fixed at compile time). */

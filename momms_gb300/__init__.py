@@ -62,6 +62,11 @@ class CallInfo(ctypes.Structure):
                 ("bound_rel_err", ctypes.c_double)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("splits", ctypes.c_int32), ("candidates", ctypes.c_int32), ("best_ms", ctypes.c_float),
+                ("reserved", ctypes.c_int32)]
+
+
 class MommsError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"momms status {status}: {message}")
@@ -106,6 +111,25 @@ def load_library(path=None):
     lib.momms_launch_count.restype = ctypes.c_ulonglong
     lib.momms_measure_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     lib.momms_measure_peak.restype = i32
+    PD = ctypes.POINTER(GemmDesc)
+    lib.momms_plan_create.argtypes = [PD, i32, ctypes.POINTER(ctypes.c_void_p)]
+    lib.momms_plan_create.restype = i32
+    lib.momms_plan_launch.argtypes = [vp, vp]
+    lib.momms_plan_launch.restype = i32
+    lib.momms_plan_capture.argtypes = [vp, vp]
+    lib.momms_plan_capture.restype = i32
+    lib.momms_plan_destroy.argtypes = [vp]
+    lib.momms_plan_destroy.restype = i32
+    lib.momms_gemm_grouped.argtypes = [PD, i32, vp]
+    lib.momms_gemm_grouped.restype = i32
+    lib.momms_autotune.argtypes = [PD, ctypes.POINTER(TuneResult), vp]
+    lib.momms_autotune.restype = i32
+    lib.momms_tune_export.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    lib.momms_tune_export.restype = i32
+    lib.momms_tune_import.argtypes = [ctypes.c_char_p]
+    lib.momms_tune_import.restype = i32
+    lib.momms_tune_clear.argtypes = []
+    lib.momms_tune_clear.restype = i32
     lib.momms_last_info.argtypes = [ctypes.POINTER(CallInfo)]
     lib.momms_last_info.restype = i32
     lib.momms_timing_enable.argtypes = [i32]

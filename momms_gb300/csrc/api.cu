@@ -62,6 +62,11 @@ DeviceState* device_state() {
       cuda_fail(e, "status word");
       return nullptr;
     }
+    int rc = set_attrs_dmma();
+    if (!rc) rc = set_attrs_grouped();
+    if (!rc) rc = set_attrs_tf32();
+    if (!rc) rc = set_attrs_ozaki();
+    if (rc) return nullptr;
     d.sm_count = sms;
     d.status = st;
     d.device = dev;

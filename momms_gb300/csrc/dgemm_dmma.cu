@@ -20,20 +20,11 @@
 // measurable.
 #include <stdio.h>
 
-#include "common.cuh"
+#include "dmma_core.cuh"
 #include "internal.h"
 
 namespace momms {
 namespace dmma {
-
-constexpr int BM = 128, BN = 128, BK = 16, STAGES = 4;
-constexpr int CONSUMER_WARPS = 8;  // 2 (m) x 4 (n)
-constexpr int THREADS = (CONSUMER_WARPS + 1) * 32;
-constexpr int CONSUMERS = CONSUMER_WARPS * 32;
-constexpr int A_STAGE = BM * BK * 8;  // bytes
-constexpr int B_STAGE = BN * BK * 8;
-constexpr int SUB = BK * 128;  // one 16-wide sub-tile of an x-contiguous operand
-constexpr int SMEM_BYTES = 1024 + STAGES * (A_STAGE + B_STAGE) + 2 * STAGES * 8 + 16;
 
 struct Params {
   int64_t m, n, k;
@@ -46,96 +37,31 @@ struct Params {
   unsigned* status;
 };
 
-// Byte offset of element (r, kk) in a k-contiguous tile: rows of 16 doubles
-// (128 bytes), 128B swizzle (16-byte chunk index XOR row mod 8).
-__device__ __forceinline__ uint32_t off_kc(int r, int kk) {
-  return r * 128 + ((((kk >> 1) ^ (r & 7))) << 4) + ((kk & 1) << 3);
-}
-// Byte offset of element (x, kk) in an x-contiguous tile stored as BM/16
-// sub-tiles of [BK rows of k][16 doubles of x], each 128B-swizzled.
-__device__ __forceinline__ uint32_t off_xc(int x, int kk) {
-  return (x >> 4) * SUB + kk * 128 + (((((x & 15) >> 1) ^ (kk & 7))) << 4) + ((x & 1) << 3);
-}
-
-__device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b) {
-  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
-               : "+d"(d0), "+d"(d1)
-               : "d"(a), "d"(b));
-}
-
-__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(CONSUMERS) : "memory"); }
-
-__device__ __forceinline__ void store_c(const Params& p, int64_t row, int64_t col, double v) {
-  if (row < p.m && col < p.n) {
-    double* cp = p.c + row * p.rsc + col * p.csc;
-    double s = v * p.alpha;
-    *cp = (p.beta == 0.0) ? s : fma(p.beta, *cp, s);
-  }
-}
-
 template <bool A_XC, bool B_XC>
 __global__ void __launch_bounds__(THREADS, 1)
     dgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params p) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + STAGES * A_STAGE;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * B_STAGE);
-  uint64_t* empty = full + STAGES;
-  int* s_last = reinterpret_cast<int*>(empty + STAGES);
-
+  const Smem sm = setup_smem(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < STAGES; ++i) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], CONSUMER_WARPS);
-    }
-    fence_barrier_init();
-  }
-  __syncthreads();
-
   const int64_t units = p.sched.units();
   const int64_t kblocks = ceil_div_dev(p.k, BK);
   const int64_t kb_split = p.sched.k_per_split / BK;
+  int stage = 0;
+  uint32_t phase = 0;
 
   if (warp == CONSUMER_WARPS) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       prefetch_tensormap(&tmA);
       prefetch_tensormap(&tmB);
-      int stage = 0;
-      uint32_t phase = 0;
       for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
         int tm, tn, sp;
         p.sched.decode(u, tm, tn, sp);
         const int64_t kb0 = sp * kb_split;
         const int64_t kb1 = min(kblocks, kb0 + kb_split);
-        for (int64_t kb = kb0; kb < kb1; ++kb) {
-          if (!mbar_wait_bounded(&empty[stage], phase ^ 1)) {
-            report_status(p.status, DEV_TIMEOUT_EMPTY);
-            return;
-          }
-          mbar_arrive_expect_tx(&full[stage], A_STAGE + B_STAGE);
-          uint8_t* a_dst = sA + stage * A_STAGE;
-          uint8_t* b_dst = sB + stage * B_STAGE;
-          const int32_t kc = (int32_t)(kb * BK);
-          if (A_XC) {
-#pragma unroll
-            for (int j = 0; j < BM / 16; ++j) tma_load_2d(a_dst + j * SUB, &tmA, &full[stage], tm * BM + 16 * j, kc);
-          } else {
-            tma_load_2d(a_dst, &tmA, &full[stage], kc, tm * BM);
-          }
-          if (B_XC) {
-#pragma unroll
-            for (int j = 0; j < BN / 16; ++j) tma_load_2d(b_dst + j * SUB, &tmB, &full[stage], tn * BN + 16 * j, kc);
-          } else {
-            tma_load_2d(b_dst, &tmB, &full[stage], kc, tn * BN);
-          }
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
-          }
-        }
+        if (!produce_unit(&tmA, &tmB, A_XC, B_XC, tm, tn, kb0, kb1, sm.sA, sm.sB, sm.full, sm.empty, stage, phase,
+                          p.status))
+          return;
       }
     }
     return;
@@ -144,102 +70,26 @@ __global__ void __launch_bounds__(THREADS, 1)
   // ---------------- DMMA consumers ----------------
   const int wm = warp >> 2;  // 0..1 -> rows wm*64
   const int wn = warp & 3;   // 0..3 -> cols wn*32
-  const int ctid = threadIdx.x;
-  int stage = 0;
-  uint32_t phase = 0;
+  const Epi e{p.m, p.n, p.alpha, p.beta, p.c, p.rsc, p.csc};
   for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
     int tm, tn, sp;
     p.sched.decode(u, tm, tn, sp);
     const int64_t kb0 = sp * kb_split;
     const int64_t kb1 = min(kblocks, kb0 + kb_split);
-
+    const int64_t row_base = (int64_t)tm * BM + wm * 64, col_base = (int64_t)tn * BN + wn * 32;
+    const uint32_t live = live_mask(row_base, col_base, p.m, p.n);
     double acc[8][4][2];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-
-    for (int64_t kb = kb0; kb < kb1; ++kb) {
-      if (!mbar_wait_bounded(&full[stage], phase)) {
-        report_status(p.status, DEV_TIMEOUT_FULL);
-        return;
-      }
-      const uint8_t* a = sA + stage * A_STAGE;
-      const uint8_t* b = sB + stage * B_STAGE;
-#pragma unroll
-      for (int ks = 0; ks < BK / 4; ++ks) {
-        const int kk = ks * 4 + (lane & 3);
-        double af[8], bf[4];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int r = wm * 64 + i * 8 + (lane >> 2);
-          af[i] = *reinterpret_cast<const double*>(a + (A_XC ? off_xc(r, kk) : off_kc(r, kk)));
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int cidx = wn * 32 + j * 8 + (lane >> 2);
-          bf[j] = *reinterpret_cast<const double*>(b + (B_XC ? off_xc(cidx, kk) : off_kc(cidx, kk)));
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[stage]);
-      if (++stage == STAGES) {
-        stage = 0;
-        phase ^= 1;
-      }
-    }
-
-    const int64_t row0 = (int64_t)tm * BM + wm * 64 + (lane >> 2);
-    const int64_t col0 = (int64_t)tn * BN + wn * 32 + 2 * (lane & 3);
-    if (p.sched.splits == 1) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-          for (int e = 0; e < 2; ++e) store_c(p, row0 + i * 8, col0 + j * 8 + e, acc[i][j][e]);
-    } else {
-      // Split-k: publish this split's partial tile; the last split to
-      // arrive sums all partials in split order 0..S-1 (a fixed order, so the
-      // result does not depend on which CTA finishes last) and writes C.
-      const int64_t tile = u / p.sched.splits;
-      const size_t tile_elems = (size_t)BM * BN;
-      double* part = p.partials + ((size_t)tile * p.sched.splits + sp) * tile_elems;
-#pragma unroll
-      for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-          for (int e = 0; e < 2; ++e) part[((i * 4 + j) * 2 + e) * CONSUMERS + ctid] = acc[i][j][e];
-      __threadfence();
-      consumer_sync();
-      if (ctid == 0) {
-        unsigned prev = atomicAdd(&p.counters[tile], 1u);
-        *s_last = (prev == (unsigned)(p.sched.splits - 1)) ? 1 : 0;
-      }
-      consumer_sync();
-      if (*s_last) {
-        __threadfence();
-        const double* base = p.partials + (size_t)tile * p.sched.splits * tile_elems;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const int r = ((i * 4 + j) * 2 + e) * CONSUMERS + ctid;
-              double s = __ldcg(base + r);
-              for (int q = 1; q < p.sched.splits; ++q) s += __ldcg(base + (size_t)q * tile_elems + r);
-              store_c(p, row0 + i * 8, col0 + j * 8 + e, s);
-            }
-        if (ctid == 0) p.counters[tile] = 0u;
-      }
-      consumer_sync();
-    }
+    if (!consume_unit(A_XC, B_XC, kb0, kb1, live, sm.sA, sm.sB, sm.full, sm.empty, stage, phase, wm, wn, lane, acc,
+                      p.status))
+      return;
+    const int64_t tile = u / p.sched.splits;
+    finish_unit(e, acc, row_base + (lane >> 2), col_base + 2 * (lane & 3), p.sched.splits, sp,
+                p.partials ? p.partials + (size_t)tile * p.sched.splits * BM * BN : nullptr,
+                p.counters ? p.counters + tile : nullptr, threadIdx.x, sm.s_last);
   }
 }
 
@@ -272,6 +122,21 @@ Orient pick_orient(const DevMat& v, int64_t rows, int64_t cols, bool x_is_rows, 
 }
 
 }  // namespace
+
+int dmma_orient(const DevMat& v, int64_t rows, int64_t cols, bool x_is_rows) {
+  return (int)pick_orient(v, rows, cols, x_is_rows, 8);
+}
+
+int set_attrs_dmma() {
+  using namespace dmma;
+  const void* kerns[4] = {(const void*)dgemm_kernel<true, true>, (const void*)dgemm_kernel<true, false>,
+                          (const void*)dgemm_kernel<false, true>, (const void*)dgemm_kernel<false, false>};
+  for (const void* kf : kerns) {
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(dgemm)");
+  }
+  return MOMMS_OK;
+}
 
 int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   using namespace dmma;
@@ -342,11 +207,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   const int64_t kblocks = ceil_div(g.k, BK);
   // Split k only when the output tiles cannot fill the GPU; each split keeps
   // at least 8 k-blocks.
-  int splits = 1;
-  if (tiles < ds->sm_count) {
-    splits = (int)std::min<int64_t>(ds->sm_count / tiles, kblocks / 8);
-    splits = std::max(1, std::min(splits, 32));
-  }
+  int splits = splits_f64(g.m, g.n, g.k, ds->sm_count);
   int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);
   p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};
@@ -366,8 +227,6 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   const int64_t units = p.sched.units();
   const int grid = (int)std::min<int64_t>(units, ds->sm_count);
   auto launch = [&](auto kern) -> cudaError_t {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return e;
     {
       KernelTimer kt(MOMMS_KERNEL_DGEMM_DMMA, s);
       kern<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
@@ -535,11 +394,7 @@ extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double
   const int tiles_m = (int)ceil_div(g.m, BM), tiles_n = (int)ceil_div(g.n, BN);
   const int64_t tiles = (int64_t)tiles_m * tiles_n;
   const int64_t kblocks = ceil_div(g.k, BK);
-  int splits = 1;
-  if (tiles < nd->sm_count) {
-    splits = (int)std::min<int64_t>(nd->sm_count / tiles, kblocks / 8);
-    splits = std::max(1, std::min(splits, 32));
-  }
+  int splits = splits_f64(g.m, g.n, g.k, nd->sm_count);
   const int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);
   p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};

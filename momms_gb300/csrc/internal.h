@@ -60,6 +60,27 @@ int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int*
 int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, void* dst, int64_t ld,
                     cudaStream_t s);
 
+// How the f64 kernels stage an operand: 0 = TMA with the non-k index
+// contiguous, 1 = TMA with k contiguous, 2 = needs a column-major repack.
+int dmma_orient(const DevMat& v, int64_t rows, int64_t cols, bool x_is_rows);
+
+// Split-k count of a plain f64 / f32 problem: from the tuning table
+// (momms_autotune) or the model. Depends only on the shape and the SM count.
+int splits_f64(int64_t m, int64_t n, int64_t k, int sm_count);
+int splits_f32(int64_t m, int64_t n, int64_t k, int sm_count);
+
+// Ozaki: choose the slice count for `d` from its target with the sampled
+// bound (synchronises `s`).
+int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s);
+
+// One-time per-device set-up of kernel attributes (dynamic shared memory
+// limits), run by device_state() so that no launch path needs it (launch
+// paths must stay legal inside stream capture).
+int set_attrs_dmma();
+int set_attrs_grouped();
+int set_attrs_tf32();
+int set_attrs_ozaki();
+
 // Record of the calling thread's current / last momms_gemm call.
 momms_call_info& call_info();
 

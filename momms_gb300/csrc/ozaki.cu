@@ -228,7 +228,85 @@ double ozaki_bound(int s, int bits, double q1, double q2) {
   return ldexp(1.0, -bits * s - 1) * (q1 + 0.5 * (s - 1) * q2);
 }
 
+// Row exponents of A (first m) and column exponents of B (next n).
+int compute_exponents(const DevGemm& g, unsigned long long* maxbits, int* exps, cudaStream_t s) {
+  const int64_t m = g.m, n = g.n, k = g.k;
+  const double* A = static_cast<const double*>(g.a.ptr);
+  const double* B = static_cast<const double*>(g.b.ptr);
+  // A viewed as m x k; B viewed transposed, n x k
+  const bool a_rc = (g.a.rs == 1 && g.a.cs != 1), b_rc = (g.b.cs == 1 && g.b.rs != 1);
+  KernelTimer kt(MOMMS_KERNEL_PREP, s);
+  cudaError_t ce = cudaMemsetAsync(maxbits, 0, (size_t)(m + n) * sizeof(unsigned long long), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
+  const dim3 blk(32, 8);
+  row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(m, 32)), blk, 0, s>>>(
+      A, g.a.rs, g.a.cs, m, k, a_rc, maxbits);
+  row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(n, 32)), blk, 0, s>>>(
+      B, g.b.cs, g.b.rs, n, k, b_rc, maxbits + m);
+  exps_kernel<<<(unsigned)ceil_div(m + n, 256), 256, 0, s>>>(maxbits, m + n, exps);
+  note_launch(3);
+  return MOMMS_OK;
+}
+
+// Smallest slice count whose sampled worst-case bound meets the target
+// (0 = FP64 level, 2^-52). Synchronises the stream once to read the sample.
+int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double target, int bits, cudaStream_t s,
+                  int* ns_out, double* bound_out) {
+  const double tgt = target > 0.0 ? target : ldexp(1.0, -52);
+  unsigned long long* q = nullptr;
+  cudaError_t ce = cudaMallocAsync(&q, 2 * sizeof(unsigned long long), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
+  cudaMemsetAsync(q, 0, 2 * sizeof(unsigned long long), s);
+  const int samples = 2048;
+  sample_bound_kernel<<<samples / 8, 256, 0, s>>>(static_cast<const double*>(g.a.ptr), g.a.rs, g.a.cs,
+                                                  static_cast<const double*>(g.b.ptr), g.b.rs, g.b.cs, g.m, g.n, g.k,
+                                                  rexp, cexp, samples, q);
+  note_launch();
+  unsigned long long hq[2] = {0, 0};
+  ce = cudaMemcpyAsync(hq, q, sizeof(hq), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  cudaFreeAsync(q, s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
+  double q1, q2;
+  memcpy(&q1, &hq[0], 8);
+  memcpy(&q2, &hq[1], 8);
+  if (!(q1 > 0.0)) q1 = 4.0;  // no usable sample (zero operands): nominal uniform-data value
+  if (!(q2 > 0.0)) q2 = 4.0;
+  int ns = 1;
+  while (ns < 16 && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
+  *ns_out = ns;
+  if (bound_out) *bound_out = ozaki_bound(ns, bits, q1, q2);
+  return MOMMS_OK;
+}
+
 }  // namespace
+
+int set_attrs_ozaki() {
+  cudaError_t e = cudaFuncSetAttribute(sp::slice_gemm_kernel<0, sp::EPI_OZAKI>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(Ozaki)");
+}
+
+int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
+  DevGemm g;
+  g.dtype = d.dtype;
+  g.m = d.m; g.n = d.n; g.k = d.k;
+  g.alpha = d.alpha; g.beta = d.beta;
+  g.a = DevMat{d.a.ptr, d.a.rs, d.a.cs};
+  g.b = DevMat{d.b.ptr, d.b.rs, d.b.cs};
+  g.c = DevMat{d.c.ptr, d.c.rs, d.c.cs};
+  void* ebuf = nullptr;
+  cudaError_t ce = cudaMallocAsync(&ebuf, (size_t)(g.m + g.n) * (sizeof(unsigned long long) + sizeof(int)), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
+  unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
+  int* exps = reinterpret_cast<int*>(maxbits + (g.m + g.n));
+  int rc = compute_exponents(g, maxbits, exps, s);
+  if (!rc) rc = choose_slices(g, exps, exps + g.m, d.target_rel_err, kDigitBits, s, slices, nullptr);
+  cudaFreeAsync(ebuf, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (!rc && e2 != cudaSuccess) rc = cuda_fail(e2, "stream synchronize");
+  return rc;
+}
 
 int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
   DeviceState* ds = device_state();
@@ -247,46 +325,15 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   int* cexp = exps + m;
   const double* A = static_cast<const double*>(g.a.ptr);
   const double* B = static_cast<const double*>(g.b.ptr);
-  {
-    // A viewed as m x k; B viewed transposed, n x k
-    const bool a_rc = (g.a.rs == 1 && g.a.cs != 1), b_rc = (g.b.cs == 1 && g.b.rs != 1);
-    KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    if ((ce = cudaMemsetAsync(maxbits, 0, (size_t)(m + n) * sizeof(unsigned long long), s)) != cudaSuccess)
-      return cuda_fail(ce, "Ozaki exponents");
-    const dim3 blk(32, 8);
-    row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(m, 32)), blk, 0, s>>>(
-        A, g.a.rs, g.a.cs, m, k, a_rc, maxbits);
-    row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(n, 32)), blk, 0, s>>>(
-        B, g.b.cs, g.b.rs, n, k, b_rc, maxbits + m);
-    exps_kernel<<<(unsigned)ceil_div(m + n, 256), 256, 0, s>>>(maxbits, m + n, exps);
-    note_launch(3);
-  }
+  int rc = compute_exponents(g, maxbits, exps, s);
+  if (rc) return rc;
 
   int ns = slices;
   if (ns <= 0) {
-    // choose from the target with the sampled bound
-    const double tgt = target > 0.0 ? target : ldexp(1.0, -52);
-    unsigned long long* q = nullptr;
-    if ((ce = cudaMallocAsync(&q, 2 * sizeof(unsigned long long), s)) != cudaSuccess)
-      return cuda_fail(ce, "Ozaki bound sample");
-    cudaMemsetAsync(q, 0, 2 * sizeof(unsigned long long), s);
-    const int samples = 2048;
-    sample_bound_kernel<<<samples / 8, 256, 0, s>>>(A, g.a.rs, g.a.cs, B, g.b.rs, g.b.cs, m, n, k, rexp, cexp,
-                                                    samples, q);
-    note_launch();
-    unsigned long long hq[2] = {0, 0};
-    ce = cudaMemcpyAsync(hq, q, sizeof(hq), cudaMemcpyDeviceToHost, s);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-    cudaFreeAsync(q, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
-    double q1, q2;
-    memcpy(&q1, &hq[0], 8);
-    memcpy(&q2, &hq[1], 8);
-    if (!(q1 > 0.0)) q1 = 4.0;  // no usable sample (zero operands): nominal uniform-data value
-    if (!(q2 > 0.0)) q2 = 4.0;
-    ns = 1;
-    while (ns < 16 && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
-    call_info().bound_rel_err = ozaki_bound(ns, bits, q1, q2);
+    double bound = 0.0;
+    rc = choose_slices(g, rexp, cexp, target, bits, s, &ns, &bound);
+    if (rc) return rc;
+    call_info().bound_rel_err = bound;
   }
   if (slices_used) *slices_used = ns;
 
@@ -378,8 +425,6 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   p.status = ds->status;
 
   auto kern = sp::slice_gemm_kernel<0, sp::EPI_OZAKI>;
-  ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
   const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
   {

@@ -27,6 +27,12 @@ struct Tf32SplitOp {
 };
 }  // namespace
 
+int set_attrs_tf32() {
+  cudaError_t e = cudaFuncSetAttribute(sp::slice_gemm_kernel<1, sp::EPI_F32>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(split-TF32)");
+}
+
 int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
@@ -84,8 +90,6 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   p.status = ds->status;
 
   auto kern = sp::slice_gemm_kernel<1, sp::EPI_F32>;
-  ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaFuncSetAttribute");
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
   const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
   {

@@ -98,3 +98,20 @@ def test_validate_mode_dtype_pairs(lib):
 def test_last_error_message(lib):
     lib.momms_gemm_validate(ctypes.byref(_desc(m=-1)))
     assert b"negative" in lib.momms_last_error()
+
+
+def test_tune_table_text_roundtrip(lib):
+    lib.momms_tune_clear()
+    assert lib.momms_tune_import(b"0 0 100 200 300 4\n1 0 64 64 9000 8\n") == mg.OK
+    need = ctypes.c_size_t(0)
+    assert lib.momms_tune_export(None, 0, ctypes.byref(need)) == mg.OK
+    buf = ctypes.create_string_buffer(need.value)
+    assert lib.momms_tune_export(buf, need.value, None) == mg.OK
+    rows = sorted(buf.value.decode().strip().split("\n"))
+    assert rows == ["0 0 100 200 300 4", "1 0 64 64 9000 8"]
+    small = ctypes.create_string_buffer(4)
+    assert lib.momms_tune_export(small, 4, None) == mg.ERR_INVALID_ARG
+    assert lib.momms_tune_import(b"garbage") == mg.ERR_INVALID_ARG
+    assert lib.momms_tune_import(b"0 0 1 1 1 99") == mg.ERR_INVALID_ARG
+    lib.momms_tune_clear()
+    assert lib.momms_tune_export(None, 0, ctypes.byref(need)) == mg.OK and need.value == 1
