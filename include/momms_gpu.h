@@ -157,6 +157,54 @@ int momms_plan_destroy(momms_plan plan);
 /* Convenience: create, launch, synchronise `stream`, destroy. */
 int momms_gemm_grouped(const momms_gemm_desc* descs, int count, void* stream);
 
+/* ---- Serving ---------------------------------------------------------------
+ * A request loop with continuous batching. Requests keep their operands
+ * resident in device memory; a request is admitted when its footprint
+ * (operands plus the work space its mode needs) fits in the HBM budget next to
+ * the requests already admitted, and is refused at submission when it could
+ * never fit. A scheduler thread launches whatever has been admitted as a
+ * grouped plan on one of `max_inflight` streams as soon as one is free, so
+ * requests arriving while others run start as slots and memory free up and
+ * overlap on the device. Results are bit-identical to momms_gemm on the same
+ * request (planning depends on a problem alone). No reference counterpart:
+ * the reference is a library of composed algorithms without a serving layer. */
+typedef struct momms_server_s* momms_server;
+typedef struct {
+  uint64_t hbm_budget_bytes; /* admission budget (0 = 60 GiB) */
+  int32_t max_batch;         /* requests per launch (0 = 64) */
+  int32_t max_inflight;      /* batches on the GPU at once (0 = 3); a request
+                                estimated over 2 ms runs alone, on at most
+                                max_inflight-1 streams, with its persistent
+                                grid capped to 3/4 of the SMs */
+  int32_t queue_capacity;    /* waiting requests before submit says BUSY (0 = 4096) */
+  int32_t reserved;
+} momms_server_config;
+typedef struct {
+  double submit_s, start_s, done_s; /* seconds on the server's clock */
+  int32_t status;                   /* momms_status of the request */
+  int32_t batch_size;               /* requests in the launch it ran in */
+} momms_request_info;
+typedef struct {
+  uint64_t submitted, completed, rejected, failed, batches;
+  double mean_batch;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submit-to-completion latency */
+  double flops_completed;                 /* 2mnk over completed requests */
+  double busy_s;                          /* first submission to last completion */
+  double tflops;                          /* flops_completed / busy_s / 1e12 */
+  uint64_t admitted_bytes;                /* footprint admitted right now */
+} momms_server_report;
+int momms_server_create(const momms_server_config* cfg, momms_server* out);
+/* MOMMS_ERR_ADMISSION: larger than the budget; MOMMS_ERR_BUSY: queue full. */
+int momms_server_submit(momms_server server, const momms_gemm_desc* desc, uint64_t* id);
+/* Request status when done (and forgets the request); MOMMS_ERR_BUSY if not. */
+int momms_server_poll(momms_server server, uint64_t id, momms_request_info* info);
+int momms_server_wait(momms_server server, uint64_t id, double timeout_s, momms_request_info* info);
+/* Waits until nothing is queued or running (MOMMS_ERR_BUSY on timeout). */
+int momms_server_drain(momms_server server, double timeout_s);
+int momms_server_stats(momms_server server, momms_server_report* out, int reset);
+/* Finishes the queued work, then stops the scheduler. */
+int momms_server_destroy(momms_server server);
+
 /* ---- Autotuning -----------------------------------------------------------
  * The runtime analogue of the reference's compile-time block sizes
  * (typenum NC/KC/MC/MR/NR, src/exper/l3_packing.rs:58-66): times the split-k

@@ -67,6 +67,24 @@ class TuneResult(ctypes.Structure):
                 ("reserved", ctypes.c_int32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("max_inflight", ctypes.c_int32),
+                ("queue_capacity", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("submit_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("status", ctypes.c_int32), ("batch_size", ctypes.c_int32)]
+
+
+class ServerReport(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("batches", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("flops_completed", ctypes.c_double), ("busy_s", ctypes.c_double),
+                ("tflops", ctypes.c_double), ("admitted_bytes", ctypes.c_uint64)]
+
+
 class MommsError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"momms status {status}: {message}")
@@ -122,6 +140,20 @@ def load_library(path=None):
     lib.momms_plan_destroy.restype = i32
     lib.momms_gemm_grouped.argtypes = [PD, i32, vp]
     lib.momms_gemm_grouped.restype = i32
+    lib.momms_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+    lib.momms_server_create.restype = i32
+    lib.momms_server_submit.argtypes = [vp, PD, ctypes.POINTER(ctypes.c_uint64)]
+    lib.momms_server_submit.restype = i32
+    lib.momms_server_poll.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(RequestInfo)]
+    lib.momms_server_poll.restype = i32
+    lib.momms_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(RequestInfo)]
+    lib.momms_server_wait.restype = i32
+    lib.momms_server_drain.argtypes = [vp, ctypes.c_double]
+    lib.momms_server_drain.restype = i32
+    lib.momms_server_stats.argtypes = [vp, ctypes.POINTER(ServerReport), i32]
+    lib.momms_server_stats.restype = i32
+    lib.momms_server_destroy.argtypes = [vp]
+    lib.momms_server_destroy.restype = i32
     lib.momms_autotune.argtypes = [PD, ctypes.POINTER(TuneResult), vp]
     lib.momms_autotune.restype = i32
     lib.momms_tune_export.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]

@@ -169,6 +169,11 @@ struct PlanProblem {
 
 struct Plan {
   int device = -1;
+  // stream-ordered mode (used by the server): allocations, uploads and frees
+  // are enqueued on `stream` instead of synchronising the device
+  bool async = false;
+  cudaStream_t stream = nullptr;
+  std::vector<char> host_tables;  // upload sources, alive until destroy
   // f64 plain group
   int nd = 0;
   int64_t d_units = 0;
@@ -206,7 +211,7 @@ int plan_alloc(Plan* p, void** out, size_t bytes) {
     *out = nullptr;
     return MOMMS_OK;
   }
-  cudaError_t e = cudaMalloc(out, bytes);
+  cudaError_t e = p->async ? cudaMallocAsync(out, bytes, p->stream) : cudaMalloc(out, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "plan allocation");
   p->allocs.push_back(*out);
   return MOMMS_OK;
@@ -214,7 +219,10 @@ int plan_alloc(Plan* p, void** out, size_t bytes) {
 
 void plan_free(Plan* p) {
   if (p->graph) cudaGraphExecDestroy(p->graph);
-  for (void* a : p->allocs) cudaFree(a);
+  for (void* a : p->allocs) {
+    if (p->async) cudaFreeAsync(a, p->stream);
+    else cudaFree(a);
+  }
   delete p;
 }
 
@@ -235,7 +243,30 @@ int set_attrs_grouped() {
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(grouped)");
 }
 
-int plan_create(const momms_gemm_desc* descs, int count, Plan** out) {
+// Copies host bytes to the device: synchronously, or stream-ordered from a
+// copy kept in the plan until it is destroyed.
+int plan_upload(Plan* p, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return MOMMS_OK;
+  cudaError_t e;
+  if (p->async) {
+    const size_t off = p->host_tables.size();
+    p->host_tables.resize(off + bytes);
+    memcpy(p->host_tables.data() + off, src, bytes);
+    (void)off;
+    e = cudaSuccess;
+  } else {
+    e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  }
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "plan upload");
+}
+
+int plan_zero(Plan* p, void* dst, size_t bytes) {
+  if (bytes == 0) return MOMMS_OK;
+  cudaError_t e = p->async ? cudaMemsetAsync(dst, 0, bytes, p->stream) : cudaMemset(dst, 0, bytes);
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "plan workspace");
+}
+
+int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_t async_stream, bool async) {
   *out = nullptr;
   if (!descs || count < 0) return fail(MOMMS_ERR_INVALID_ARG, "descs is null or count < 0");
   DeviceState* ds = device_state();
@@ -252,6 +283,9 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out) {
   }
   Plan* p = new Plan();
   p->device = ds->device;
+  p->async = async;
+  p->stream = async_stream;
+  std::vector<std::pair<void*, std::pair<size_t, size_t>>> pending;  // (dst, (offset, bytes)) of async uploads
 
   std::vector<int> dlist, slist;
   for (int i = 0; i < count; ++i) {
@@ -378,10 +412,14 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out) {
     if (!rc) { p->d_partials = static_cast<double*>(buf); rc = plan_alloc(p, &buf, (size_t)ctrs * 4); }
     if (!rc) p->d_counters = static_cast<unsigned*>(buf);
     if (rc) { plan_free(p); return rc; }
-    cudaError_t e = cudaMemcpy(p->d_probs, probs.data(), probs.size() * sizeof(grouped::DProblem), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(p->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && ctrs) e = cudaMemset(p->d_counters, 0, (size_t)ctrs * 4);
-    if (e != cudaSuccess) { plan_free(p); return cuda_fail(e, "plan upload"); }
+    size_t off = p->host_tables.size();
+    rc = plan_upload(p, p->d_probs, probs.data(), probs.size() * sizeof(grouped::DProblem));
+    if (!rc && async) pending.push_back({p->d_probs, {off, probs.size() * sizeof(grouped::DProblem)}});
+    off = p->host_tables.size();
+    if (!rc) rc = plan_upload(p, p->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap));
+    if (!rc && async) pending.push_back({p->d_maps, {off, maps.size() * sizeof(CUtensorMap)}});
+    if (!rc) rc = plan_zero(p, p->d_counters, (size_t)ctrs * 4);
+    if (rc) { plan_free(p); return rc; }
   }
 
   // ---- f32 group ----
@@ -438,10 +476,12 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out) {
     if (!rc) { p->s_counters = static_cast<unsigned*>(buf); rc = plan_alloc(p, &buf, 2 * sizeof(unsigned long long)); }
     if (!rc) p->s_next = static_cast<unsigned long long*>(buf);
     if (rc) { plan_free(p); return rc; }
-    cudaError_t e = cudaMemcpy(p->s_probs, probs.data(), probs.size() * sizeof(grouped::SProblem), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(p->s_counters, 0, (size_t)ctrs * 4 + 16);
-    if (e == cudaSuccess) e = cudaMemset(p->s_next, 0, 2 * sizeof(unsigned long long));
-    if (e != cudaSuccess) { plan_free(p); return cuda_fail(e, "plan upload"); }
+    const size_t off = p->host_tables.size();
+    rc = plan_upload(p, p->s_probs, probs.data(), probs.size() * sizeof(grouped::SProblem));
+    if (!rc && async) pending.push_back({p->s_probs, {off, probs.size() * sizeof(grouped::SProblem)}});
+    if (!rc) rc = plan_zero(p, p->s_counters, (size_t)ctrs * 4 + 16);
+    if (!rc) rc = plan_zero(p, p->s_next, 2 * sizeof(unsigned long long));
+    if (rc) { plan_free(p); return rc; }
   }
 
   // Ozaki problems with a data-chosen slice count: choose once now (one
@@ -449,16 +489,28 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out) {
   for (PlanProblem& pp : p->other) {
     if (pp.d.precision == MOMMS_PREC_OZAKI && pp.slices == 0) {
       int s = 0;
-      int rc = ozaki_choose_slices(pp.d, &s, 0);
+      int rc = ozaki_choose_slices(pp.d, &s, async ? async_stream : nullptr);
       if (rc) { plan_free(p); return rc; }
       pp.slices = s;
+    }
+  }
+  // stream-ordered uploads: the host copies live in p->host_tables (no more
+  // appends from here on, so the addresses are stable)
+  for (auto& pu : pending) {
+    cudaError_t e = cudaMemcpyAsync(pu.first, p->host_tables.data() + pu.second.first, pu.second.second,
+                                    cudaMemcpyHostToDevice, async_stream);
+    if (e != cudaSuccess) {
+      plan_free(p);
+      return cuda_fail(e, "plan upload");
     }
   }
   *out = p;
   return MOMMS_OK;
 }
 
-int plan_launch(Plan* p, cudaStream_t s) {
+void plan_destroy(Plan* p) { plan_free(p); }
+
+int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   if (ds->device != p->device) return fail(MOMMS_ERR_INVALID_ARG, "plan belongs to device %d", p->device);
@@ -468,7 +520,8 @@ int plan_launch(Plan* p, cudaStream_t s) {
     if (rc) return rc;
   }
   if (p->nd) {
-    const int grid = (int)std::min<int64_t>(p->d_units, ds->sm_count);
+    const int sms = (max_sms > 0 && max_sms < ds->sm_count) ? max_sms : ds->sm_count;
+    const int grid = (int)std::min<int64_t>(p->d_units, sms);
     KernelTimer kt(MOMMS_KERNEL_DGEMM_DMMA, s);
     grouped::dgemm_grouped_kernel<<<grid, dmma::THREADS, dmma::SMEM_BYTES, s>>>(
         p->d_maps, p->d_probs, p->nd, p->d_units, p->d_partials, p->d_counters, ds->status);
@@ -476,7 +529,8 @@ int plan_launch(Plan* p, cudaStream_t s) {
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f64 launch");
   }
   if (p->ns) {
-    const int grid = (int)std::min<int64_t>(p->s_units, 2 * ds->sm_count);
+    const int sms = (max_sms > 0 && max_sms < ds->sm_count) ? max_sms : ds->sm_count;
+    const int grid = (int)std::min<int64_t>(p->s_units, 2 * sms);
     KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
     grouped::sgemm_grouped_kernel<<<grid, ffma::THREADS, 0, s>>>(p->s_probs, p->ns, p->s_units, p->s_next,
                                                                  p->s_partials, p->s_counters);
@@ -518,7 +572,7 @@ int momms_plan_create(const momms_gemm_desc* descs, int count, momms_plan* out) 
   if (!out) return momms::fail(MOMMS_ERR_INVALID_ARG, "out is null");
   *out = nullptr;
   momms::Plan* p = nullptr;
-  int rc = momms::plan_create(descs, count, &p);
+  int rc = momms::plan_create(descs, count, &p, nullptr, false);
   if (rc) return rc;
   *out = new momms_plan_s{p};
   return MOMMS_OK;
@@ -531,7 +585,7 @@ int momms_plan_launch(momms_plan plan, void* stream) {
     cudaError_t e = cudaGraphLaunch(plan->p->graph, s);
     return e == cudaSuccess ? MOMMS_OK : momms::cuda_fail(e, "cudaGraphLaunch");
   }
-  return momms::plan_launch(plan->p, s);
+  return momms::plan_launch(plan->p, s, 0);
 }
 
 int momms_plan_capture(momms_plan plan, void* stream) {
@@ -547,7 +601,7 @@ int momms_plan_capture(momms_plan plan, void* stream) {
     cudaStreamDestroy(s);
     return momms::cuda_fail(e, "cudaStreamBeginCapture");
   }
-  int rc = momms::plan_launch(p, s);
+  int rc = momms::plan_launch(p, s, 0);
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(s, &g);
   cudaStreamDestroy(s);

@@ -81,6 +81,15 @@ int set_attrs_grouped();
 int set_attrs_tf32();
 int set_attrs_ozaki();
 
+// Execution plans (grouped.cu). With `async`, allocations, uploads and frees
+// are stream-ordered on `stream` (no device-wide synchronisation); otherwise
+// plan_create is synchronous.
+struct Plan;
+int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_t stream, bool async);
+// max_sms > 0 caps the persistent grids, leaving SMs for concurrent work.
+int plan_launch(Plan* p, cudaStream_t s, int max_sms);
+void plan_destroy(Plan* p);
+
 // Record of the calling thread's current / last momms_gemm call.
 momms_call_info& call_info();
 
