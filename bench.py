@@ -20,6 +20,12 @@ The metric is FP64 GEMM throughput at FP64 accuracy, plain vs emulated:
   cpu_baseline : the reference's Goto algorithm on the host cores (the
           oracle's restatement; the reference's own asm kernels where they can
           run), on a bounded sample of the same workload.
+  batched : 512 uneven problems as one captured grouped plan vs one launch
+          per problem;
+  serving : the served request stream (Poisson arrivals, mixed sizes and
+          modes) with p50/p99 latency and throughput against the offline
+          grouped run of the same requests (served_p50_ms / served_p99_ms
+          repeat the first rate's figures).
 
 --impl reference runs only that CPU algorithm, with every host thread, and
 prints its own line.
@@ -56,6 +62,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--size", type=int, default=M, help="m = n = k (default 8192)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the batched and serving measurements")
     return p.parse_args()
 
 
@@ -297,6 +304,112 @@ def _kernel_ms(lib, mg, cls):
     return tot.value, cnt.value
 
 
+def _problem_set(mg, torch, dev, count, lo, hi, seed, kinds_p):
+    """Device-resident requests: m, n, k log-uniform over [lo, hi], kinds drawn
+    with probabilities kinds_p over (f64 plain, f64 emulated at 1e-14, f32)."""
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice(3, count, p=kinds_p)
+    dims = np.exp(rng.uniform(np.log(lo), np.log(hi), (count, 3))).astype(np.int64)
+    descs = (mg.GemmDesc * count)()
+    keep = []
+    flops = 0.0
+    for i in range(count):
+        m, n, k = (int(x) for x in dims[i])
+        f32 = kinds[i] == 2
+        dt = torch.float32 if f32 else torch.float64
+        A = (torch.rand((k, m), dtype=dt, device=dev) * 2 - 1).t()
+        B = (torch.rand((n, k), dtype=dt, device=dev) * 2 - 1).t()
+        C = (torch.rand((n, m), dtype=dt, device=dev) * 2 - 1).t()
+        d = mg.GemmDesc()
+        d.dtype = mg.DTYPE_F32 if f32 else mg.DTYPE_F64
+        d.precision = mg.PREC_OZAKI if kinds[i] == 1 else mg.PREC_PLAIN
+        d.m, d.n, d.k = m, n, k
+        d.alpha, d.beta = 1.0, 1.0
+        d.a = mg.Operand(A.data_ptr(), 1, m, mg.MEM_DEVICE, 0)
+        d.b = mg.Operand(B.data_ptr(), 1, k, mg.MEM_DEVICE, 0)
+        d.c = mg.Operand(C.data_ptr(), 1, m, mg.MEM_DEVICE, 0)
+        d.target_rel_err = 1e-14 if kinds[i] == 1 else 0.0
+        descs[i] = d
+        keep.append((A, B, C))
+        flops += 2.0 * m * n * k
+    return descs, keep, flops
+
+
+def _time_on(torch, stream, fn, reps):
+    fn()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measure_batched(lib, mg, torch, dev):
+    """512 uneven problems (m, n, k log-uniform over [32, 1024], half f64 and
+    half f32, plain) as one plan launched through its CUDA graph, against one
+    momms_gemm launch per problem."""
+    count = 512
+    descs, keep, flops = _problem_set(mg, torch, dev, count, 32, 1024, 512, [0.5, 0.0, 0.5])
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    plan = ctypes.c_void_p()
+    mg.check(lib.momms_plan_create(descs, count, ctypes.byref(plan)), lib)
+    mg.check(lib.momms_plan_capture(plan, sp), lib)
+    t_graph = _time_on(torch, stream, lambda: mg.check(lib.momms_plan_launch(plan, sp), lib), 5)
+
+    def singles():
+        for i in range(count):
+            mg.check(lib.momms_gemm(ctypes.byref(descs[i]), sp), lib)
+    t_single = _time_on(torch, stream, singles, 2)
+    lib.momms_plan_destroy(plan)
+    del keep
+    return {"workload": "512 problems, m,n,k log-uniform [32,1024] (seed 512), half f64 half f32, plain",
+            "grouped_graph_ms": t_graph, "per_problem_launches_ms": t_single,
+            "grouped_tflops": flops / (t_graph * 1e-3) / 1e12, "speedup_vs_per_problem": t_single / t_graph,
+            "launches_per_batch": "one graph launch (one persistent kernel per dtype)"}
+
+
+def measure_serving(lib, mg, torch, dev, rates=(400.0, 1600.0), count=300):
+    """Poisson arrivals of mixed requests (m, n, k log-uniform over [64, 4096];
+    40% f64 plain, 40% f64 emulated at a 1e-14 target, 20% f32) with operands
+    resident in HBM under a 60 GiB budget; latency percentiles and throughput
+    against the offline grouped run of the same request set."""
+    descs, keep, flops = _problem_set(mg, torch, dev, count, 64, 4096, 5, [0.4, 0.4, 0.2])
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    plan = ctypes.c_void_p()
+    mg.check(lib.momms_plan_create(descs, count, ctypes.byref(plan)), lib)
+    off_ms = _time_on(torch, stream, lambda: mg.check(lib.momms_plan_launch(plan, sp), lib), 1)
+    lib.momms_plan_destroy(plan)
+    offline = flops / (off_ms * 1e-3) / 1e12
+    runs = []
+    for rate in rates:
+        cfg = mg.ServerConfig(hbm_budget_bytes=60 << 30, max_batch=64, max_inflight=3, queue_capacity=100000)
+        srv = ctypes.c_void_p()
+        mg.check(lib.momms_server_create(ctypes.byref(cfg), ctypes.byref(srv)), lib)
+        arrivals = np.cumsum(np.random.default_rng(9).exponential(1.0 / rate, count))
+        t0 = time.perf_counter()
+        for i in range(count):
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            rid = ctypes.c_uint64(0)
+            mg.check(lib.momms_server_submit(srv, ctypes.byref(descs[i]), ctypes.byref(rid)), lib)
+        mg.check(lib.momms_server_drain(srv, 300.0), lib)
+        rep = mg.ServerReport()
+        lib.momms_server_stats(srv, ctypes.byref(rep), 0)
+        lib.momms_server_destroy(srv)
+        runs.append({"rate_per_s": rate, "p50_ms": rep.p50_ms, "p99_ms": rep.p99_ms, "mean_ms": rep.mean_ms,
+                     "tflops": rep.tflops, "vs_offline_grouped": rep.tflops / offline, "batches": rep.batches,
+                     "mean_batch": rep.mean_batch, "completed": rep.completed, "failed": rep.failed})
+    del keep
+    return {"workload": f"{count} requests, Poisson arrivals, m,n,k log-uniform [64,4096] (seed 5), "
+                        "40% f64 plain / 40% f64 emulated (1e-14) / 20% f32, 60 GiB admission budget",
+            "offline_grouped_tflops": offline, "runs": runs}
+
+
 def _measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -432,6 +545,15 @@ def run_ours(args):
         "clocks": clk,
         "wall_s_timed": t_wall,
     }
+    if not args.no_extras:
+        line["batched"] = measure_batched(lib, mg, torch, dev)
+        line["serving"] = measure_serving(lib, mg, torch, dev)
+        serving_runs = line["serving"]["runs"]
+        line["served_p50_ms"] = serving_runs[0]["p50_ms"]
+        line["served_p99_ms"] = serving_runs[0]["p99_ms"]
+    bits = ctypes.c_uint32(0)
+    lib.momms_device_status(ctypes.byref(bits))
+    line["device_status_bits"] = bits.value
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, rows, dt, kind = cpu_reference(A, B, C0, budget_s=10.0, threads=threads)
