@@ -67,11 +67,35 @@ DeviceState* device_state() {
     if (!rc) rc = set_attrs_tf32();
     if (!rc) rc = set_attrs_ozaki();
     if (rc) return nullptr;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) {
+      cuda_fail(e, "scratch pool");
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    d.pool = pool;
     d.sm_count = sms;
     d.status = st;
     d.device = dev;
   }
   return &d;
+}
+
+cudaError_t scratch_alloc_raw(void** ptr, size_t bytes, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    cs = cudaStreamCaptureStatusNone;
+  }
+  DeviceState* d = (cs == cudaStreamCaptureStatusNone) ? device_state() : nullptr;
+  if (d && d->pool) return cudaMallocFromPoolAsync(ptr, bytes, d->pool, s);
+  return cudaMallocAsync(ptr, bytes, s);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -204,7 +228,7 @@ int stage_in(const momms_operand& op, int64_t rows, int64_t cols, size_t es, boo
   st.row_major = (op.cs == 1 && op.rs != 1);
   const int64_t inner = st.row_major ? cols : rows, outer = st.row_major ? rows : cols;
   st.ld = round_up(std::max<int64_t>(inner, 1), 16 / (int64_t)es);
-  cudaError_t e = cudaMallocAsync(&st.owned, (size_t)st.ld * std::max<int64_t>(outer, 1) * es, s);
+  cudaError_t e = scratch_alloc(&st.owned, (size_t)st.ld * std::max<int64_t>(outer, 1) * es, s);
   if (e != cudaSuccess) return cuda_fail(e, "staging buffer");
   st.dev = st.row_major ? DevMat{st.owned, st.ld, 1} : DevMat{st.owned, 1, st.ld};
   if (!copy || rows == 0 || cols == 0) return MOMMS_OK;

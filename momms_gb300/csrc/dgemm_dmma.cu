@@ -151,7 +151,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   Orient ob = pick_orient(g.b, g.k, g.n, false, 8);
   if (oa == ORIENT_REPACK) {
     int64_t ld = round_up(g.m, 2);
-    if ((ce = cudaMallocAsync(&scratch[0], (size_t)ld * g.k * 8, s)) != cudaSuccess) return cuda_fail(ce, "scratch A");
+    if ((ce = scratch_alloc(&scratch[0], (size_t)ld * g.k * 8, s)) != cudaSuccess) return cuda_fail(ce, "scratch A");
     int rc = repack_colmajor(g.a, g.m, g.k, 8, scratch[0], ld, s);
     if (rc) return rc;
     g.a = DevMat{scratch[0], 1, ld};
@@ -159,7 +159,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   }
   if (ob == ORIENT_REPACK) {
     int64_t ld = round_up(g.k, 2);
-    if ((ce = cudaMallocAsync(&scratch[1], (size_t)ld * g.n * 8, s)) != cudaSuccess) return cuda_fail(ce, "scratch B");
+    if ((ce = scratch_alloc(&scratch[1], (size_t)ld * g.n * 8, s)) != cudaSuccess) return cuda_fail(ce, "scratch B");
     int rc = repack_colmajor(g.b, g.k, g.n, 8, scratch[1], ld, s);
     if (rc) return rc;
     g.b = DevMat{scratch[1], 1, ld};
@@ -218,7 +218,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   if (splits > 1) {
     size_t part_bytes = (size_t)tiles * splits * BM * BN * 8;
     size_t cnt_bytes = (size_t)tiles * 4;
-    if ((ce = cudaMallocAsync(&ws, part_bytes + cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "split-k workspace");
+    if ((ce = scratch_alloc(&ws, part_bytes + cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "split-k workspace");
     p.partials = static_cast<double*>(ws);
     p.counters = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + part_bytes);
     if ((ce = cudaMemsetAsync(p.counters, 0, cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "memset counters");

@@ -211,7 +211,7 @@ int plan_alloc(Plan* p, void** out, size_t bytes) {
     *out = nullptr;
     return MOMMS_OK;
   }
-  cudaError_t e = p->async ? cudaMallocAsync(out, bytes, p->stream) : cudaMalloc(out, bytes);
+  cudaError_t e = p->async ? scratch_alloc(out, bytes, p->stream) : cudaMalloc(out, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "plan allocation");
   p->allocs.push_back(*out);
   return MOMMS_OK;

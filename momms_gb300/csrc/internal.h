@@ -15,7 +15,19 @@ struct DeviceState {
   int device = -1;
   int sm_count = 0;
   unsigned* status = nullptr;  // device status word (see DEV_* bits)
+  cudaMemPool_t pool = nullptr;  // the library's stream-ordered scratch pool
 };
+
+// Stream-ordered scratch allocation (free with cudaFreeAsync) from the
+// library's own pool, which keeps freed memory reserved instead of returning
+// it to the driver at every synchronisation (the default pool's behaviour,
+// which made each large call re-map its scratch). Inside stream capture it
+// falls back to cudaMallocAsync (graph memory nodes).
+cudaError_t scratch_alloc_raw(void** ptr, size_t bytes, cudaStream_t s);
+template <typename T>
+inline cudaError_t scratch_alloc(T** ptr, size_t bytes, cudaStream_t s) {
+  return scratch_alloc_raw(reinterpret_cast<void**>(ptr), bytes, s);
+}
 
 // Returns the state of the calling thread's current device (initialising it
 // on first use), or nullptr with the error recorded.

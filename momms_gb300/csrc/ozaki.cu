@@ -151,33 +151,44 @@ struct OzakiSliceOp {
 //   q1 = (2^e_i sum|b_.j| + 2^f_j sum|a_i.|) / (|A||B|)_ij
 //   q2 = k 2^(e_i+f_j) / (|A||B|)_ij
 // reduced to their maxima in out[0], out[1] (as ordered non-negative floats).
-__global__ void sample_bound_kernel(const double* __restrict__ a, int64_t rsa, int64_t csa,
-                                    const double* __restrict__ b, int64_t rsb, int64_t csb, int64_t m, int64_t n,
-                                    int64_t k, const int* __restrict__ rexp, const int* __restrict__ cexp,
-                                    int samples, unsigned long long* out) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= samples) return;
-  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(warp + 1);
+// Block (r, c) samples 32 consecutive rows of A against one column of B:
+// lanes walk the rows (coalesced for column-major A), warps split k.
+constexpr int kSampleRowBlocks = 8, kSampleCols = 8;
+__global__ void __launch_bounds__(256) sample_bound_kernel(const double* __restrict__ a, int64_t rsa, int64_t csa,
+                                                           const double* __restrict__ b, int64_t rsb, int64_t csb,
+                                                           int64_t m, int64_t n, int64_t k,
+                                                           const int* __restrict__ rexp, const int* __restrict__ cexp,
+                                                           unsigned long long* out) {
+  __shared__ double s_ab[8][32], s_a[8][32], s_b[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(blockIdx.x * 131 + blockIdx.y * 7 + 1);
   h ^= h >> 31;
   h *= 0xBF58476D1CE4E5B9ull;
   h ^= h >> 29;
-  const int64_t i = (int64_t)(h % (uint64_t)m);
-  const int64_t j = (int64_t)((h >> 20) % (uint64_t)n);
+  const int64_t i0 = m > 32 ? (int64_t)(h % (uint64_t)(m - 31)) : 0;
+  const int64_t j = (int64_t)((h >> 24) % (uint64_t)n);
+  const int64_t i = i0 + lane;
   double sab = 0.0, sa = 0.0, sb = 0.0;
-  for (int64_t pp = lane; pp < k; pp += 32) {
-    const double av = fabs(a[i * rsa + pp * csa]);
+  for (int64_t pp = warp; pp < k; pp += 8) {
     const double bv = fabs(b[pp * rsb + j * csb]);
-    sab += av * bv;
-    sa += av;
     sb += bv;
+    if (i < m) {
+      const double av = fabs(a[i * rsa + pp * csa]);
+      sab += av * bv;
+      sa += av;
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    sab += __shfl_xor_sync(0xffffffffu, sab, o);
-    sa += __shfl_xor_sync(0xffffffffu, sa, o);
-    sb += __shfl_xor_sync(0xffffffffu, sb, o);
-  }
-  if (lane == 0) {
+  s_ab[warp][lane] = sab;
+  s_a[warp][lane] = sa;
+  if (lane == 0) s_b[warp] = sb;
+  __syncthreads();
+  if (warp == 0 && i < m) {
+    for (int w = 1; w < 8; ++w) {
+      sab += s_ab[w][lane];
+      sa += s_a[w][lane];
+    }
+    sb = 0.0;
+    for (int w = 0; w < 8; ++w) sb += s_b[w];
     const int ei = rexp[i], fj = cexp[j];
     if (ei == INT32_MAX || fj == INT32_MAX || sab == 0.0) return;
     const double q1 = (ldexp(sb, ei) + ldexp(sa, fj)) / sab;
@@ -188,15 +199,20 @@ __global__ void sample_bound_kernel(const double* __restrict__ a, int64_t rsa, i
   }
 }
 
-// FP64 recombination of the exact group sums (Horner from the smallest
-// weight): R = S_g + w_g R with w_g = 2^-bits at the first group of a new
-// diagonal and 1 inside a split diagonal; then
-// C = beta*C + alpha * 2^(e_i + f_j - 2 bits) * R.
+// Recombination of the exact group sums. Group g holds S_g = the int32 sum of
+// the digit products of diagonal d_g (weight 2^(-bits*(d_g-2))), so
+//   R = sum_g S_g * 2^(bits*(dmax - (d_g-2)))
+// is an exact integer (below 2^(30 + bits*dmax + log2 groups) < 2^127), and
+//   C = beta*C + alpha * 2^(e_i + f_j - 2 bits - bits*dmax) * R
+// with R rounded to double once. All the summation is integer arithmetic;
+// FP64 is used for the final conversion, scaling and beta update only.
 struct CombineParams {
   const int* sbuf;
   int64_t plane;
   int ngroups;
-  uint8_t shift[sp::MAX_GROUPS];
+  int dmax;                     // min(largest d_g - 2, 12): R stays below 2^127; lower
+                                // diagonals lose bits beyond 2^(-12 bits) of the top one
+  uint8_t dgrp[sp::MAX_GROUPS];  // d_g - 2 per group
   int64_t m, n;
   const int* row_exp;
   const int* col_exp;
@@ -206,17 +222,40 @@ struct CombineParams {
   int64_t rsc, csc;
 };
 
+// Nearest double to a 128-bit signed integer times 2^scale.
+__device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
+  if (R == 0) return 0.0;
+  const bool neg = R < 0;
+  unsigned __int128 U = neg ? (unsigned __int128)(-R) : (unsigned __int128)R;
+  const unsigned long long hi = (unsigned long long)(U >> 64);
+  unsigned long long top;
+  int sh = 0;
+  if (hi == 0) {
+    top = (unsigned long long)U;
+  } else {
+    sh = 64 - __clzll((long long)hi);  // significant bits above the low word
+    top = (unsigned long long)(U >> sh);
+    const unsigned __int128 rest = U & (((unsigned __int128)1 << sh) - 1);
+    if (rest != 0) top |= 1ull;  // sticky bit: top keeps 64 significant bits
+  }
+  const double v = __ull2double_rn(top);  // the only rounding
+  return ldexp(neg ? -v : v, sh + scale);
+}
+
 __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
   const int64_t total = p.m * p.n;
-  const double down = ldexp(1.0, -p.bits);
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e % p.m, j = e / p.m;
-    double R = 0.0;
-    for (int g = 0; g < p.ngroups; ++g) R = fma(p.shift[g] ? down : 1.0, R, (double)p.sbuf[g * p.plane + e]);
+    __int128 R = 0;
+    for (int g = 0; g < p.ngroups; ++g) {
+      const int sh = p.bits * (p.dmax - p.dgrp[g]);
+      const __int128 Sg = (__int128)p.sbuf[g * p.plane + e];
+      R += sh >= 0 ? (Sg << sh) : (Sg >> (-sh));
+    }
     const int er = p.row_exp[i], ec = p.col_exp[j];
     double v;
     if (er == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-    else v = ldexp(R, er + ec - 2 * p.bits);
+    else v = i128_to_double(R, er + ec - 2 * p.bits - p.bits * p.dmax);
     double* cp = p.c + i * p.rsc + j * p.csc;
     const double sv = v * p.alpha;
     *cp = (p.beta == 0.0) ? sv : fma(p.beta, *cp, sv);
@@ -254,13 +293,12 @@ int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double tar
                   int* ns_out, double* bound_out) {
   const double tgt = target > 0.0 ? target : ldexp(1.0, -52);
   unsigned long long* q = nullptr;
-  cudaError_t ce = cudaMallocAsync(&q, 2 * sizeof(unsigned long long), s);
+  cudaError_t ce = scratch_alloc(&q, 2 * sizeof(unsigned long long), s);
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
   cudaMemsetAsync(q, 0, 2 * sizeof(unsigned long long), s);
-  const int samples = 2048;
-  sample_bound_kernel<<<samples / 8, 256, 0, s>>>(static_cast<const double*>(g.a.ptr), g.a.rs, g.a.cs,
-                                                  static_cast<const double*>(g.b.ptr), g.b.rs, g.b.cs, g.m, g.n, g.k,
-                                                  rexp, cexp, samples, q);
+  sample_bound_kernel<<<dim3(kSampleRowBlocks, kSampleCols), 256, 0, s>>>(
+      static_cast<const double*>(g.a.ptr), g.a.rs, g.a.cs, static_cast<const double*>(g.b.ptr), g.b.rs, g.b.cs, g.m,
+      g.n, g.k, rexp, cexp, q);
   note_launch();
   unsigned long long hq[2] = {0, 0};
   ce = cudaMemcpyAsync(hq, q, sizeof(hq), cudaMemcpyDeviceToHost, s);
@@ -296,7 +334,7 @@ int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
   g.b = DevMat{d.b.ptr, d.b.rs, d.b.cs};
   g.c = DevMat{d.c.ptr, d.c.rs, d.c.cs};
   void* ebuf = nullptr;
-  cudaError_t ce = cudaMallocAsync(&ebuf, (size_t)(g.m + g.n) * (sizeof(unsigned long long) + sizeof(int)), s);
+  cudaError_t ce = scratch_alloc(&ebuf, (size_t)(g.m + g.n) * (sizeof(unsigned long long) + sizeof(int)), s);
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
   unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
   int* exps = reinterpret_cast<int*>(maxbits + (g.m + g.n));
@@ -317,7 +355,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
 
   // exponents: [m + n] u64 maxima followed by [m + n] int exponents
   void* ebuf = nullptr;
-  if ((ce = cudaMallocAsync(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
+  if ((ce = scratch_alloc(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki exponents");
   unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
   int* exps = reinterpret_cast<int*>(maxbits + (m + n));
@@ -340,7 +378,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int64_t kp = round_up(k, 8);  // 16-byte rows of fp16
   const size_t a_plane = (size_t)m * kp, b_plane = (size_t)n * kp;
   __half* planes_buf = nullptr;
-  if ((ce = cudaMallocAsync(&planes_buf, (size_t)ns * (a_plane + b_plane) * sizeof(__half), s)) != cudaSuccess)
+  if ((ce = scratch_alloc(&planes_buf, (size_t)ns * (a_plane + b_plane) * sizeof(__half), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki slice planes");
   __half* pa = planes_buf;
   __half* pb = planes_buf + (size_t)ns * a_plane;
@@ -401,7 +439,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       if (ng >= sp::MAX_GROUPS) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
       p.group_begin[ng] = np;
       p.chunk_kb[ng] = chunk;
-      cp.shift[ng] = (i0 == 0 && ng > 0) ? 1 : 0;
+      cp.dgrp[ng] = (uint8_t)(d - 2);
       for (int i = i0; i < std::min(nt, i0 + pairs_per_group); ++i) {
         p.pair_a[np] = (uint8_t)(tlist[i] - 1);
         p.pair_b[np] = (uint8_t)(d - tlist[i] - 1);
@@ -418,7 +456,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
 
   int* sbuf = nullptr;
   const size_t plane = (size_t)m * n;
-  if ((ce = cudaMallocAsync(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
+  if ((ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki group sums");
   p.sbuf = sbuf;
   p.plane = (int64_t)plane;
@@ -436,6 +474,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.sbuf = sbuf;
   cp.plane = (int64_t)plane;
   cp.ngroups = ng;
+  cp.dmax = std::min(ns - 1, 12);
   cp.m = m;
   cp.n = n;
   cp.row_exp = rexp;

@@ -68,14 +68,14 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   auto unit = [](const DevMat& v, int64_t, int64_t) { return v.rs == 1 || v.cs == 1; };
   if (!unit(g.a, g.m, g.k)) {
     int64_t ld = round_up(g.m, 4);
-    if ((ce = cudaMallocAsync(&scratch[0], (size_t)ld * g.k * 4, s)) != cudaSuccess) return cuda_fail(ce, "scratch A");
+    if ((ce = scratch_alloc(&scratch[0], (size_t)ld * g.k * 4, s)) != cudaSuccess) return cuda_fail(ce, "scratch A");
     int rc = repack_colmajor(g.a, g.m, g.k, 4, scratch[0], ld, s);
     if (rc) return rc;
     g.a = DevMat{scratch[0], 1, ld};
   }
   if (!unit(g.b, g.k, g.n)) {
     int64_t ld = round_up(g.k, 4);
-    if ((ce = cudaMallocAsync(&scratch[1], (size_t)ld * g.n * 4, s)) != cudaSuccess) return cuda_fail(ce, "scratch B");
+    if ((ce = scratch_alloc(&scratch[1], (size_t)ld * g.n * 4, s)) != cudaSuccess) return cuda_fail(ce, "scratch B");
     int rc = repack_colmajor(g.b, g.k, g.n, 4, scratch[1], ld, s);
     if (rc) return rc;
     g.b = DevMat{scratch[1], 1, ld};
@@ -108,7 +108,7 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   if (splits > 1) {
     size_t part_bytes = (size_t)tiles * splits * BM * BN * 4;
     size_t cnt_bytes = (size_t)tiles * 4;
-    if ((ce = cudaMallocAsync(&ws, part_bytes + cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "split-k workspace");
+    if ((ce = scratch_alloc(&ws, part_bytes + cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "split-k workspace");
     p.partials = static_cast<float*>(ws);
     p.counters = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + part_bytes);
     if ((ce = cudaMemsetAsync(p.counters, 0, cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "memset counters");

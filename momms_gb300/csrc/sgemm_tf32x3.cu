@@ -39,7 +39,7 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   const int64_t kp = round_up(g.k, 4);  // 16-byte rows for TMA
   const size_t a_plane = (size_t)g.m * kp, b_plane = (size_t)g.n * kp;
   void* buf = nullptr;
-  cudaError_t ce = cudaMallocAsync(&buf, (2 * a_plane + 2 * b_plane) * sizeof(float), s);
+  cudaError_t ce = scratch_alloc(&buf, (2 * a_plane + 2 * b_plane) * sizeof(float), s);
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 planes");
   float* pa = static_cast<float*>(buf);
   float* pb = pa + 2 * a_plane;

@@ -64,6 +64,20 @@ struct Params {
 
 __device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0; }
 
+// Output tile of work item t: groups of 16 m-tiles swept n-tile by n-tile,
+// so that the ~152 tiles in flight at once share 16 A row panels and about
+// 10 B column panels of each slice plane in L2 (a plain column-major sweep
+// would touch a whole 128 MB plane per pair at m = 8192).
+__device__ __forceinline__ void tile_coords(int64_t t, int tiles_m, int tiles_n, int& tm, int& tn) {
+  constexpr int G = 16;
+  const int64_t per_group = (int64_t)G * tiles_n;
+  const int64_t g = t / per_group, r = t % per_group;
+  const int first = (int)(g * G);
+  const int gm = min(G, tiles_m - first);
+  tm = first + (int)(r % gm);
+  tn = (int)(r / gm);
+}
+
 // f32 integer value |x| <= 2^22 -> int32 via the 1.5*2^23 magic constant
 __device__ __forceinline__ int f2i_exact(uint32_t bits) {
   const float f = __uint_as_float(bits) + 12582912.0f;
@@ -119,7 +133,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t armed = 0;  // bit s: stage s has been armed at least once
       uint32_t last_ph = 0;  // bit s: parity of the phase last armed on stage s
       for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
-        const int tm = (int)(t % p.tiles_m), tn = (int)(t / p.tiles_m);
+        int tm, tn;
+        tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
         for (int g = 0; g < p.ngroups; ++g) {
           for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
             for (int kb = 0; kb < p.kblocks; ++kb) {
@@ -209,7 +224,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     int buf = 0;
     uint32_t acc_ph[2] = {0, 0};
     for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
-      const int tm = (int)(t % p.tiles_m), tn = (int)(t / p.tiles_m);
+      int tm, tn;
+      tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
       // per-thread accumulators of finished chunks: exact int32 digit sums
