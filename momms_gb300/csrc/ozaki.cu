@@ -103,10 +103,12 @@ __global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int6
 // Signed digits of v * 2^-e at `bits` bits each, nearest rounding at the last
 // digit: X = round(|v| * 2^(bits*slices - e)) as an integer, then centred
 // digits are peeled from the bottom (each in [-2^(bits-1), 2^(bits-1))) and the
-// remaining top digit lies in [0, 2^bits]. Returns the digits of |v|; the
-// caller applies the sign. U is uint64 (bits*slices <= 62) or __int128.
+// remaining top digit lies in [0, 2^bits]. Digit t (sign applied) goes to
+// out[t * plane_elems] as it is produced. U is uint64 (bits*slices <= 62) or
+// __int128.
 template <typename U>
-__device__ __forceinline__ void digits_of(unsigned long long ab, int e, int bits, int slices, int* d) {
+__device__ __forceinline__ void write_digits(unsigned long long ab, bool neg, int e, int bits, int slices, __half* out,
+                                             int64_t plane_elems) {
   const unsigned long long frac = ab & ((1ull << 52) - 1);
   const int be = (int)(ab >> 52);
   const unsigned long long M = be ? (frac | (1ull << 52)) : frac;
@@ -120,10 +122,10 @@ __device__ __forceinline__ void digits_of(unsigned long long ab, int e, int bits
   for (int t = slices - 1; t >= 1; --t) {
     const U low = X & mask;
     const int dt = (low >= half) ? (int)low - (1 << bits) : (int)low;
-    d[t] = dt;
+    out[(int64_t)t * plane_elems] = __int2half_rn(neg ? -dt : dt);
     X = (dt < 0) ? ((X + (U)(-dt)) >> bits) : ((X - (U)dt) >> bits);
   }
-  d[0] = (int)X;
+  out[0] = __int2half_rn(neg ? -(int)X : (int)X);
 }
 
 struct OzakiSliceOp {
@@ -133,17 +135,15 @@ struct OzakiSliceOp {
   int bits;
   __device__ __forceinline__ void operator()(double v, int64_t r, __half* out, int64_t plane_elems) const {
     const int e = exps[r];
-    int d[16];
     const unsigned long long ab = abs_bits(v);
-    if (e == INT32_MAX || ab == 0) {
-      for (int t = 0; t < slices; ++t) d[t] = 0;
-    } else if (bits * slices <= 62) {
-      digits_of<unsigned long long>(ab, e, bits, slices, d);
-    } else {
-      digits_of<unsigned __int128>(ab, e, bits, slices, d);
-    }
     const bool neg = __double_as_longlong(v) < 0;
-    for (int t = 0; t < slices; ++t) out[(int64_t)t * plane_elems] = __int2half_rn(neg ? -d[t] : d[t]);
+    if (e == INT32_MAX || ab == 0) {
+      for (int t = 0; t < slices; ++t) out[(int64_t)t * plane_elems] = __int2half_rn(0);
+    } else if (bits * slices <= 62) {
+      write_digits<unsigned long long>(ab, neg, e, bits, slices, out, plane_elems);
+    } else {
+      write_digits<unsigned __int128>(ab, neg, e, bits, slices, out, plane_elems);
+    }
   }
 };
 

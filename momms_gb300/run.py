@@ -1,0 +1,65 @@
+"""Run one GEMM configuration repeatedly on the GPU (timing and profiling aid).
+
+    python -m momms_gb300.run --m 4096 --n 4096 --k 4096 --dtype f64 --prec ozaki --reps 3
+
+Operands are device-resident, column-major, uniform [-1, 1] from a fixed
+seed; C starts equal to A*B-sized random data and beta = 1. Prints one JSON
+line with the mean device time per call (CUDA events) and TFLOP/s.
+"""
+import argparse
+import ctypes
+import json
+
+import momms_gb300 as mg
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--m", type=int, default=4096)
+    p.add_argument("--n", type=int, default=4096)
+    p.add_argument("--k", type=int, default=4096)
+    p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
+    p.add_argument("--prec", choices=["plain", "ozaki", "tf32"], default="plain")
+    p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--target", type=float, default=0.0)
+    p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=1)
+    a = p.parse_args()
+
+    import torch
+    lib = mg.load_library()
+    dt = torch.float64 if a.dtype == "f64" else torch.float32
+    g = torch.Generator(device="cuda").manual_seed(1234)
+    A = (torch.rand((a.k, a.m), dtype=dt, device="cuda", generator=g) * 2 - 1).t()
+    B = (torch.rand((a.n, a.k), dtype=dt, device="cuda", generator=g) * 2 - 1).t()
+    C = (torch.rand((a.n, a.m), dtype=dt, device="cuda", generator=g) * 2 - 1).t()
+    d = mg.GemmDesc()
+    d.dtype = mg.DTYPE_F64 if a.dtype == "f64" else mg.DTYPE_F32
+    d.precision = {"plain": mg.PREC_PLAIN, "ozaki": mg.PREC_OZAKI, "tf32": mg.PREC_SPLIT_TF32}[a.prec]
+    d.m, d.n, d.k = a.m, a.n, a.k
+    d.alpha, d.beta = 1.0, 1.0
+    d.a = mg.Operand(A.data_ptr(), 1, a.m, mg.MEM_DEVICE, 0)
+    d.b = mg.Operand(B.data_ptr(), 1, a.k, mg.MEM_DEVICE, 0)
+    d.c = mg.Operand(C.data_ptr(), 1, a.m, mg.MEM_DEVICE, 0)
+    d.slices = a.slices
+    d.target_rel_err = a.target
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    for _ in range(a.warmup):
+        mg.check(lib.momms_gemm(ctypes.byref(d), sp), lib)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(a.reps):
+        mg.check(lib.momms_gemm(ctypes.byref(d), sp), lib)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, a.reps)
+    info = mg.CallInfo()
+    lib.momms_last_info(ctypes.byref(info))
+    print(json.dumps({"m": a.m, "n": a.n, "k": a.k, "dtype": a.dtype, "prec": a.prec, "ms": ms,
+                      "tflops": 2.0 * a.m * a.n * a.k / (ms * 1e-3) / 1e12, "slices": info.slices,
+                      "pairs": info.pairs, "splits": info.splits}))
+
+
+if __name__ == "__main__":
+    main()
