@@ -79,6 +79,12 @@ DeviceState* device_state() {
     }
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaStream_t cs = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) {
+      cuda_fail(e, "copy stream");
+      return nullptr;
+    }
+    d.copy_stream = cs;
     d.pool = pool;
     d.sm_count = sms;
     d.status = st;
@@ -219,22 +225,37 @@ struct Staged {
   int64_t ld = 0;
 };
 
-// Host -> device copy of a rows x cols view into an owned buffer.
-int stage_in(const momms_operand& op, int64_t rows, int64_t cols, size_t es, bool copy, Staged& st, cudaStream_t s) {
+// Device buffer for a rows x cols host view (column-major unless the view is
+// row-major), allocated in stream order on `s`.
+int stage_alloc(const momms_operand& op, int64_t rows, int64_t cols, size_t es, Staged& st, cudaStream_t s) {
   st.rows = rows;
   st.cols = cols;
   st.host = true;
-  // column-major copy unless the source is row-major
   st.row_major = (op.cs == 1 && op.rs != 1);
   const int64_t inner = st.row_major ? cols : rows, outer = st.row_major ? rows : cols;
   st.ld = round_up(std::max<int64_t>(inner, 1), 16 / (int64_t)es);
   cudaError_t e = scratch_alloc(&st.owned, (size_t)st.ld * std::max<int64_t>(outer, 1) * es, s);
   if (e != cudaSuccess) return cuda_fail(e, "staging buffer");
   st.dev = st.row_major ? DevMat{st.owned, st.ld, 1} : DevMat{st.owned, 1, st.ld};
-  if (!copy || rows == 0 || cols == 0) return MOMMS_OK;
-  const int64_t src_inner_stride = st.row_major ? op.cs : op.rs;
-  const int64_t src_outer_stride = st.row_major ? op.rs : op.cs;
-  if (src_inner_stride == 1 && (outer == 1 || src_outer_stride >= inner)) {
+  return MOMMS_OK;
+}
+
+// A host view whose unit stride runs along the staged buffer's inner index
+// and whose other stride leaves room for it: copied with one 2-D memcpy.
+bool plain_pitch(const momms_operand& op, const Staged& st) {
+  const int64_t inner = st.row_major ? st.cols : st.rows, outer = st.row_major ? st.rows : st.cols;
+  const int64_t in_stride = st.row_major ? op.cs : op.rs, out_stride = st.row_major ? op.rs : op.cs;
+  return in_stride == 1 && (outer == 1 || out_stride >= inner);
+}
+
+// Host -> device copy of the view into its staging buffer, on stream `s`.
+int stage_copy_in(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s) {
+  const int64_t rows = st.rows, cols = st.cols;
+  if (rows == 0 || cols == 0) return MOMMS_OK;
+  const int64_t inner = st.row_major ? cols : rows, outer = st.row_major ? rows : cols;
+  cudaError_t e;
+  if (plain_pitch(op, st)) {
+    const int64_t src_outer_stride = st.row_major ? op.rs : op.cs;
     const size_t spitch = (size_t)(outer == 1 ? inner : src_outer_stride) * es;
     e = cudaMemcpy2DAsync(st.owned, (size_t)st.ld * es, op.ptr, spitch, (size_t)inner * es, (size_t)outer,
                           cudaMemcpyHostToDevice, s);
@@ -254,6 +275,25 @@ int stage_in(const momms_operand& op, int64_t rows, int64_t cols, size_t es, boo
   // the vector must outlive the copy
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "H2D copy");
+  return MOMMS_OK;
+}
+
+// Device -> host copy of columns [j0, j1) of a staged C whose host view has a
+// plain pitch (plain_pitch), on stream `s`.
+int stage_out_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s) {
+  if (st.rows == 0 || j1 <= j0) return MOMMS_OK;
+  cudaError_t e;
+  if (st.row_major) {  // each row holds columns j0..j1 contiguously
+    e = cudaMemcpy2DAsync(static_cast<char*>(op.ptr) + (size_t)j0 * es, (size_t)(st.rows == 1 ? st.cols : op.rs) * es,
+                          static_cast<const char*>(st.owned) + (size_t)j0 * es, (size_t)st.ld * es,
+                          (size_t)(j1 - j0) * es, (size_t)st.rows, cudaMemcpyDeviceToHost, s);
+  } else {  // columns j0..j1, each contiguous
+    e = cudaMemcpy2DAsync(static_cast<char*>(op.ptr) + (size_t)j0 * op.cs * es,
+                          (size_t)(st.cols == 1 ? st.rows : op.cs) * es,
+                          static_cast<const char*>(st.owned) + (size_t)j0 * st.ld * es, (size_t)st.ld * es,
+                          (size_t)st.rows * es, (size_t)(j1 - j0), cudaMemcpyDeviceToHost, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "D2H copy");
   return MOMMS_OK;
 }
 
@@ -281,6 +321,31 @@ int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t
              es);
     }
   return MOMMS_OK;
+}
+
+// Per-call staging state: the hooks the launchers see, the copy stream and
+// events (0-2: A, B, C copied in; 3: buffers allocated; 4: copies done).
+struct StagedCall {
+  Staging hooks;
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t cols_ev = nullptr;  // C columns final on the compute stream (re-recorded per range)
+  const momms_operand* c_op = nullptr;
+  const Staged* c_st = nullptr;
+  size_t es = 0;
+  ~StagedCall() {
+    if (cols_ev) cudaEventDestroy(cols_ev);
+  }
+};
+
+int writeback_cols(Staging* h, int64_t j0, int64_t j1, cudaStream_t s) {
+  StagedCall* sc = static_cast<StagedCall*>(h->ctx);
+  cudaError_t e = cudaSuccess;
+  if (!sc->cols_ev) e = cudaEventCreateWithFlags(&sc->cols_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(sc->cols_ev, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(sc->copy, sc->cols_ev, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "C copy-back");
+  return stage_out_cols(*sc->c_op, sc->es, *sc->c_st, j0, j1, sc->copy);
 }
 
 int dispatch(const DevGemm& g, const momms_gemm_desc* d, cudaStream_t s) {
@@ -323,24 +388,75 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   g.beta = d->beta;
   Staged st[3];
   DevMat* dm[3] = {&g.a, &g.b, &g.c};
+  const bool any_host = host[0] || host[1] || host[2];
+  bool need[3];
   for (int i = 0; i < 3; ++i) {
-    if (host[i]) {
-      const bool copy = (i < 2) || (d->beta != 0.0);
-      rc = stage_in(*ops[i], rows[i], cols[i], es, copy, st[i], s);
-      if (rc) break;
-      *dm[i] = st[i].dev;
-    } else {
-      *dm[i] = DevMat{ops[i]->ptr, ops[i]->rs, ops[i]->cs};
-    }
+    need[i] = host[i] && (i < 2 || d->beta != 0.0);  // C is read only when beta != 0
+    if (!host[i]) *dm[i] = DevMat{ops[i]->ptr, ops[i]->rs, ops[i]->cs};
   }
+  for (int i = 0; i < 3 && !rc; ++i)
+    if (host[i]) {
+      rc = stage_alloc(*ops[i], rows[i], cols[i], es, st[i], s);
+      if (!rc) *dm[i] = st[i].dev;
+    }
+
+  // Staging overlap: the host->device copies run on the device's copy stream
+  // while the kernels that do not need them yet run on `s`; C comes back per
+  // column range. Not inside stream capture (the call synchronises anyway).
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (any_host && cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
+  DeviceState* ds = device_state();
+  const bool overlap = any_host && cap == cudaStreamCaptureStatusNone && ds && ds->copy_stream;
+  StagedCall sc;
+  sc.copy = overlap ? ds->copy_stream : s;
+  sc.c_op = ops[2];
+  sc.c_st = &st[2];
+  sc.es = es;
+  if (!rc && overlap) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sc.ev[i], cudaEventDisableTiming);
+    // the copy stream starts after the staging buffers exist (allocated on s)
+    if (e == cudaSuccess) e = cudaEventRecord(sc.ev[3], s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(sc.copy, sc.ev[3], 0);
+    if (e != cudaSuccess) rc = cuda_fail(e, "staging events");
+    for (int i = 0; i < 3 && !rc; ++i)
+      if (need[i]) {
+        rc = stage_copy_in(*ops[i], es, st[i], sc.copy);
+        if (!rc && (e = cudaEventRecord(sc.ev[i], sc.copy)) != cudaSuccess) rc = cuda_fail(e, "staging events");
+        if (!rc) sc.hooks.ready[i] = sc.ev[i];
+      }
+    if (host[2] && plain_pitch(*ops[2], st[2])) {
+      sc.hooks.writeback = writeback_cols;
+      sc.hooks.ctx = &sc;
+    }
+    g.staging = &sc.hooks;
+  } else {
+    for (int i = 0; i < 3 && !rc; ++i)
+      if (need[i]) rc = stage_copy_in(*ops[i], es, st[i], s);
+  }
+
   if (!rc) rc = dispatch(g, d, s);
-  if (!rc && host[2]) rc = stage_out(*ops[2], es, st[2], s);
+  if (!rc && host[2]) {
+    if (sc.hooks.writeback) rc = columns_done(g, sc.hooks.written, g.n, s);  // what the path left
+    else rc = stage_out(*ops[2], es, st[2], s);
+  }
+  if (overlap && sc.ev[4]) {
+    // s (and so the frees below) waits for everything on the copy stream
+    cudaError_t e = cudaEventRecord(sc.ev[4], sc.copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, sc.ev[4], 0);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "staging events");
+  }
   for (int i = 0; i < 3; ++i)
     if (st[i].owned) cudaFreeAsync(st[i].owned, s);
-  if (host[0] || host[1] || host[2]) {
+  if (any_host) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (!rc && e != cudaSuccess) rc = cuda_fail(e, "stream synchronize");
   }
+  for (int i = 0; i < 5; ++i)
+    if (sc.ev[i]) cudaEventDestroy(sc.ev[i]);
   if (!rc) g_last_info = g_info;
   return rc;
 }

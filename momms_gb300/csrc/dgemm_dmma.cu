@@ -145,6 +145,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   DevGemm g = g0;
   void* scratch[2] = {nullptr, nullptr};
   cudaError_t ce;
+  if ((ce = wait_operands(g, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
 
   // A: rows m, cols k, x = m. B: rows k, cols n, x = n.
   Orient oa = pick_orient(g.a, g.m, g.k, true, 8);

@@ -16,6 +16,7 @@ struct DeviceState {
   int sm_count = 0;
   unsigned* status = nullptr;  // device status word (see DEV_* bits)
   cudaMemPool_t pool = nullptr;  // the library's stream-ordered scratch pool
+  cudaStream_t copy_stream = nullptr;  // host<->device staging copies of momms_gemm calls
 };
 
 // Stream-ordered scratch allocation (free with cudaFreeAsync) from the
@@ -50,13 +51,45 @@ struct DevMat {
   int64_t rs, cs;
 };
 
-// One GEMM with all operands already on the device.
+// A call whose operands are being staged from host memory: their
+// host->device copies run on a separate copy stream, and each kernel sequence
+// waits (on its own stream) only for the operand it is about to read. C's
+// device->host copy can start per column range as soon as that range is final.
+struct Staging {
+  cudaEvent_t ready[3] = {nullptr, nullptr, nullptr};  // A, B, C copied in; null = already on the device
+  // Enqueues the copy-back of C's columns [j0, j1), final in stream order on
+  // `s`; null when C is device memory or needs a host-side scatter.
+  int (*writeback)(Staging* st, int64_t j0, int64_t j1, cudaStream_t s) = nullptr;
+  void* ctx = nullptr;
+  int64_t written = 0;  // columns of C handed to writeback so far
+};
+
+// One GEMM with all operands on the device (or arriving there, see Staging).
 struct DevGemm {
   int dtype;  // momms_dtype
   int64_t m, n, k;
   double alpha, beta;
   DevMat a, b, c;
+  Staging* staging = nullptr;
 };
+
+// Make `s` wait until operand `which` (0 = A, 1 = B, 2 = C) is on the device.
+inline cudaError_t wait_operand(const DevGemm& g, int which, cudaStream_t s) {
+  if (!g.staging || !g.staging->ready[which]) return cudaSuccess;
+  return cudaStreamWaitEvent(s, g.staging->ready[which], 0);
+}
+inline cudaError_t wait_operands(const DevGemm& g, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = wait_operand(g, i, s);
+  return e;
+}
+// C's columns [j0, j1) are final in stream order on `s`.
+inline int columns_done(const DevGemm& g, int64_t j0, int64_t j1, cudaStream_t s) {
+  if (!g.staging || !g.staging->writeback || j1 <= j0) return 0;
+  int rc = g.staging->writeback(g.staging, j0, j1, s);
+  if (!rc) g.staging->written = j1;
+  return rc;
+}
 
 // Launchers for the plain paths (device operands; asynchronous on `s`).
 int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s);

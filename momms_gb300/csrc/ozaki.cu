@@ -220,6 +220,7 @@ struct CombineParams {
   double alpha, beta;
   double* c;
   int64_t rsc, csc;
+  int64_t e_begin, e_end;  // entries [e_begin, e_end) of C in column order (e = i + j*m)
 };
 
 // Nearest double to a 128-bit signed integer times 2^scale.
@@ -243,8 +244,8 @@ __device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
 }
 
 __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
-  const int64_t total = p.m * p.n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = p.e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < p.e_end;
+       e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e % p.m, j = e / p.m;
     __int128 R = 0;
     for (int g = 0; g < p.ngroups; ++g) {
@@ -363,6 +364,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   int* cexp = exps + m;
   const double* A = static_cast<const double*>(g.a.ptr);
   const double* B = static_cast<const double*>(g.b.ptr);
+  if ((ce = wait_operand(g, 0, s)) != cudaSuccess || (ce = wait_operand(g, 1, s)) != cudaSuccess)
+    return cuda_fail(ce, "operand staging");
   int rc = compute_exponents(g, maxbits, exps, s);
   if (rc) return rc;
 
@@ -485,15 +488,24 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.c = static_cast<double*>(g.c.ptr);
   cp.rsc = g.c.rs;
   cp.csc = g.c.cs;
-  const int64_t total = (int64_t)plane;
-  const int cblocks = (int)std::min<int64_t>(ceil_div(total, 256), (int64_t)ds->sm_count * 16);
-  {
-    KernelTimer kt(MOMMS_KERNEL_COMBINE, s);
-    combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+  if ((ce = wait_operand(g, 2, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+  // With C staged from host memory the recombination runs in column ranges,
+  // each copied back while the next is computed.
+  const int64_t nchunks = (g.staging && g.staging->writeback) ? std::min<int64_t>(4, n) : 1;
+  for (int64_t ch = 0; ch < nchunks; ++ch) {
+    const int64_t j0 = n * ch / nchunks, j1 = n * (ch + 1) / nchunks;
+    cp.e_begin = j0 * m;
+    cp.e_end = j1 * m;
+    const int cblocks = (int)std::min<int64_t>(ceil_div(cp.e_end - cp.e_begin, 256), (int64_t)ds->sm_count * 16);
+    {
+      KernelTimer kt(MOMMS_KERNEL_COMBINE, s);
+      combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+    }
+    note_launch();
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
+    if ((rc = columns_done(g, j0, j1, s)) != 0) return rc;
   }
-  note_launch();
-  ce = cudaGetLastError();
-  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
   cudaFreeAsync(planes_buf, s);
   cudaFreeAsync(sbuf, s);
   cudaFreeAsync(ebuf, s);

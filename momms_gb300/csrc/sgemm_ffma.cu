@@ -63,6 +63,7 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   DevGemm g = g0;
   void* scratch[2] = {nullptr, nullptr};
   cudaError_t ce;
+  if ((ce = wait_operands(g, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   // A must have unit stride along m or k; B along k or n. Anything else is
   // first copied into a column-major scratch matrix.
   auto unit = [](const DevMat& v, int64_t, int64_t) { return v.rs == 1 || v.cs == 1; };

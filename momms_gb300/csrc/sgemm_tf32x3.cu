@@ -43,10 +43,16 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 planes");
   float* pa = static_cast<float*>(buf);
   float* pb = pa + 2 * a_plane;
+  // each operand's split waits only for that operand (timers exclude the waits)
+  if ((ce = wait_operand(g, 0, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   {
     KernelTimer kt(MOMMS_KERNEL_PREP, s);
     planes::launch_to_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, (int64_t)a_plane,
                              Tf32SplitOp{}, s);
+  }
+  if ((ce = wait_operand(g, 1, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+  {
+    KernelTimer kt(MOMMS_KERNEL_PREP, s);
     planes::launch_to_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, (int64_t)b_plane,
                              Tf32SplitOp{}, s);
   }
@@ -89,6 +95,8 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   p.csc = g.c.cs;
   p.status = ds->status;
 
+  // the epilogue reads C
+  if ((ce = wait_operand(g, 2, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   auto kern = sp::slice_gemm_kernel<1, sp::EPI_F32>;
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
   const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
