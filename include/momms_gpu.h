@@ -130,6 +130,29 @@ int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, co
                         int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
                         int64_t rs_c, int64_t cs_c, void* stream);
 
+/* ---- Out-of-core (host-resident) GEMMs -----------------------------------
+ * A momms_gemm call with host operands whose staged copies plus work space
+ * would exceed the staging budget is computed in blocks: C in mb x nb blocks,
+ * k in slabs of kb (later slabs accumulate with beta = 1, as the reference's
+ * PartK does), the operand blocks streamed through two device slots each
+ * while the previous block computes and the one before is copied back. The
+ * reference's counterpart is its out-of-core / L4 blocking of PartM / PartN
+ * above the in-cache algorithm (src/exper/out_of_core.rs:77-87,
+ * src/exper/l4.rs:71-78). Each block is an independent device GEMM: with an
+ * automatic Ozaki slice count every block meets the target on its own; with
+ * k in one slab and a fixed slice count the Ozaki result is bit-identical to
+ * the unblocked call.
+ *
+ * Budget in bytes (0 = automatic: the device's free memory, plus what the
+ * library's pool holds unused, less max(1 GiB, 5 %)). Process-wide. */
+int momms_set_staging_budget(uint64_t bytes);
+uint64_t momms_staging_budget(void);
+/* The blocking a call would use under `budget` (0 = the budget in effect),
+ * without running it; operands flagged MOMMS_MEM_AUTO count as host memory.
+ * mb = m, nb = n, kb = k when the call fits unblocked. MOMMS_ERR_OUT_OF_MEMORY
+ * if no blocking fits. */
+int momms_stream_plan(const momms_gemm_desc* desc, uint64_t budget, int64_t* mb, int64_t* nb, int64_t* kb);
+
 /* ---- Grouped launches and execution plans --------------------------------
  * Many independent GEMMs run as one persistent kernel per dtype: every plain
  * f64 problem's tiles (and k-splits) are work units of one DMMA kernel, every

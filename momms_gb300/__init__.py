@@ -168,6 +168,13 @@ def load_library(path=None):
     lib.momms_timing_enable.restype = i32
     lib.momms_timing_read.argtypes = [i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_ulonglong), i32]
     lib.momms_timing_read.restype = i32
+    lib.momms_set_staging_budget.argtypes = [ctypes.c_uint64]
+    lib.momms_set_staging_budget.restype = i32
+    lib.momms_staging_budget.argtypes = []
+    lib.momms_staging_budget.restype = ctypes.c_uint64
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    lib.momms_stream_plan.argtypes = [PD, ctypes.c_uint64, i64p, i64p, i64p]
+    lib.momms_stream_plan.restype = i32
     if path is None:
         _lib = lib
     return lib

@@ -16,7 +16,8 @@ struct DeviceState {
   int sm_count = 0;
   unsigned* status = nullptr;  // device status word (see DEV_* bits)
   cudaMemPool_t pool = nullptr;  // the library's stream-ordered scratch pool
-  cudaStream_t copy_stream = nullptr;  // host<->device staging copies of momms_gemm calls
+  cudaStream_t copy_stream = nullptr;   // host->device staging copies of momms_gemm calls
+  cudaStream_t copy_stream2 = nullptr;  // device->host copies of streamed (out-of-core) calls
 };
 
 // Stream-ordered scratch allocation (free with cudaFreeAsync) from the
@@ -91,6 +92,52 @@ inline int columns_done(const DevGemm& g, int64_t j0, int64_t j1, cudaStream_t s
   return rc;
 }
 
+// ---- Staging of host operand views (staging.cu) ----
+bool is_device_ptr(const void* p);
+// The device copy of a host view: column-major unless the view is row-major,
+// leading dimension rounded up to 16 bytes.
+struct Staged {
+  DevMat dev{};
+  void* owned = nullptr;
+  bool host = false;
+  int64_t rows = 0, cols = 0;
+  bool row_major = false;  // layout of the device copy
+  int64_t ld = 0;
+};
+int stage_alloc(const momms_operand& op, int64_t rows, int64_t cols, size_t es, Staged& st, cudaStream_t s);
+// The view's unit stride runs along the device copy's inner index with room
+// for it: one 2-D memcpy each way (otherwise the host gathers / scatters).
+bool plain_pitch(const momms_operand& op, const Staged& st);
+int stage_copy_in(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s);
+int stage_out_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s);
+int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s);
+
+// Runs one GEMM on device (or arriving, see Staging) operands with the
+// precision mode of `d` (api.cu).
+int run_device_gemm(const DevGemm& g, const momms_gemm_desc& d, cudaStream_t s);
+
+// Device bytes a mode needs beyond the operands for an m x n x k problem
+// (slice planes, group sums, split-k partials); an upper bound.
+size_t work_bytes(int dtype, int precision, int slices, int64_t m, int64_t n, int64_t k);
+
+// ---- Out-of-core blocking (outofcore.cu) ----
+// Block sizes of a streamed call: C in mb x nb blocks, k in slabs of kb,
+// `order_m_outer` = loop over row blocks outside column blocks.
+struct BlockPlan {
+  int64_t mb = 0, nb = 0, kb = 0;
+  bool order_m_outer = false;
+  size_t bytes = 0;           // device bytes the plan holds
+  double host_traffic = 0.0;  // host<->device bytes it moves
+};
+int plan_blocks(const momms_gemm_desc& d, const bool host[3], uint64_t budget, BlockPlan* out);
+// Device bytes an unblocked call holds: staged host operands + work space.
+size_t incore_bytes(const momms_gemm_desc& d, const bool host[3]);
+// The staging budget in effect (momms_set_staging_budget, or the device's
+// free memory less a margin).
+uint64_t staging_budget();
+// C := beta*C + alpha*A*B with at least one host operand, streamed in blocks.
+int gemm_streamed(const momms_gemm_desc& d, const bool host[3], const BlockPlan& plan, cudaStream_t s);
+
 // Launchers for the plain paths (device operands; asynchronous on `s`).
 int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s);
 int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s);
@@ -98,6 +145,8 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s);
 // Ozaki FP64 emulation: target relative error (0 = FP64 level) and slice count
 // (0 = chosen from the target). *slices_used receives the count actually used.
 int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int* slices_used, cudaStream_t s);
+// Accumulation groups (int32 sum planes) of an ns-slice product with this k.
+int ozaki_group_count(int ns, int64_t k);
 
 // Copy an operand into a column-major device scratch matrix with an even
 // leading dimension (used when its strides or alignment do not suit TMA or

@@ -35,6 +35,7 @@ namespace momms {
 namespace {
 
 constexpr int kDigitBits = 7;
+constexpr int64_t kMaxK = 65536;  // k per launch: int32 digit sums stay exact up to 2^16 products
 
 // Everything in the pre-pass runs on integer bit patterns: GB300's FP64 pipe
 // is about 1 TFLOP/s, so FP64 arithmetic per element would dominate.
@@ -347,9 +348,51 @@ int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
   return rc;
 }
 
+int ozaki_group_count(int ns, int64_t k) {
+  // the launcher's schedule below: one group per diagonal d = t + u, split
+  // where a diagonal's int32 sums could pass 2^30
+  const int bits = kDigitBits;
+  const double kblocks = (double)ceil_div(std::min<int64_t>(std::max<int64_t>(k, 1), kMaxK), 64);
+  int ng = 0;
+  for (int d = 2; d <= ns + 1; ++d) {
+    int nt = 0;
+    double maxprod = 0.0;
+    for (int t = 1; t <= ns; ++t) {
+      const int u = d - t;
+      if (u < 1 || u > ns) continue;
+      ++nt;
+      maxprod = fmax(maxprod, ldexp(1.0, t == 1 ? bits : bits - 1) * ldexp(1.0, u == 1 ? bits : bits - 1));
+    }
+    const int ppg = (int)std::max(1.0, floor(ldexp(1.0, 30) / (kblocks * 64.0 * maxprod)));
+    ng += (nt + ppg - 1) / ppg;
+  }
+  return ng;
+}
+
 int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
+  if (g.k > kMaxK) {
+    // k slabs of at most 2^16 (the int32 digit sums' range), later slabs
+    // accumulating into C with beta = 1 like the reference's PartK
+    // (src/composables/part.rs:96-110); each slab meets the target on its own
+    const int64_t nslab = ceil_div(g.k, kMaxK), kb = round_up(ceil_div(g.k, nslab), 64);
+    for (int64_t p0 = 0; p0 < g.k; p0 += kb) {
+      DevGemm gs = g;
+      gs.k = std::min(kb, g.k - p0);
+      gs.a.ptr = static_cast<double*>(g.a.ptr) + p0 * g.a.cs;
+      gs.b.ptr = static_cast<double*>(g.b.ptr) + p0 * g.b.rs;
+      if (p0 > 0) {
+        gs.beta = 1.0;
+        gs.staging = nullptr;  // the first slab waited for the operands
+      } else if (g.staging) {
+        gs.staging->writeback = nullptr;  // C goes back after the last slab
+      }
+      int rc = launch_dgemm_ozaki(gs, target, slices, slices_used, s);
+      if (rc) return rc;
+    }
+    return MOMMS_OK;
+  }
   const int bits = kDigitBits;
   const int64_t m = g.m, n = g.n, k = g.k;
   cudaError_t ce;
@@ -392,7 +435,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   }
   note_launch(2);
 
-  if (k > 65536) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 (int32 digit sums)");
+  if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 per launch");
   CUtensorMap tmA, tmB;
   {
     uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)ns};

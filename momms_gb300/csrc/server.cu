@@ -63,16 +63,7 @@ double estimate_s(const momms_gemm_desc& d) {
 size_t footprint_of(const momms_gemm_desc& d) {
   const size_t es = d.dtype == MOMMS_DTYPE_F64 ? 8 : 4;
   const double m = (double)d.m, n = (double)d.n, k = (double)d.k;
-  double bytes = es * (m * k + k * n + m * n);
-  if (d.precision == MOMMS_PREC_OZAKI) {
-    const double s = d.slices > 0 ? d.slices : 9;  // FP64-level targets take up to 9 slices
-    bytes += 2.0 * s * (m + n) * k + 4.0 * s * m * n + 12.0 * (m + n);
-  } else if (d.precision == MOMMS_PREC_SPLIT_TF32) {
-    bytes += 8.0 * (m + n) * k;
-  } else {
-    bytes += 21.0 * 1024 * 1024;  // split-k partials: at most one 128 x 128 tile per SM
-  }
-  return (size_t)bytes;
+  return (size_t)(es * (m * k + k * n + m * n)) + work_bytes(d.dtype, d.precision, d.slices, d.m, d.n, d.k);
 }
 
 }  // namespace
