@@ -26,6 +26,8 @@
 #include <cuda_fp16.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "internal.h"
 #include "planes.cuh"
 #include "slicegemm.cuh"
@@ -101,81 +103,152 @@ __global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int6
   exps[i] = e;
 }
 
-// Signed digits of v * 2^-e at `bits` bits each, nearest rounding at the last
-// digit: X = round(|v| * 2^(bits*slices - e)) as an integer, then centred
-// digits are peeled from the bottom (each in [-2^(bits-1), 2^(bits-1))) and the
-// remaining top digit lies in [0, 2^bits]. Digit t (sign applied) goes to
-// out[t * plane_elems] as it is produced. U is uint64 (bits*slices <= 62) or
-// __int128.
-template <typename U>
-__device__ __forceinline__ void write_digits(unsigned long long ab, bool neg, int e, int bits, int slices, __half* out,
-                                             int64_t plane_elems) {
+// Signed digits of v * 2^-e at kDigitBits bits each, nearest rounding at the
+// last digit: X = round(|v| * 2^(bits*NS - e)) as an integer, written as
+//   X = sum_{pos < NS-1} d_pos 2^(bits*pos) + top 2^(bits*(NS-1))
+// with centred lower digits d_pos in [-2^(bits-1), 2^(bits-1)) and the top
+// digit in [0, 2^bits]. That representation is unique, and all its digits come
+// at once from Y = X + H, H = 2^(bits-1) * sum_{pos < NS-1} 2^(bits*pos):
+// Y's plain base-2^bits digits are u_pos = d_pos + 2^(bits-1), and its bits
+// above position bits*(NS-1) are the top digit. Zero, and every element of a
+// row holding a NaN or an infinity (e == INT32_MAX), get X = 0: all digits 0.
+// U is uint64 (bits*NS <= 62) or __int128.
+template <int NS, typename U>
+__device__ __forceinline__ U offset_digits(double v, int e) {
+  constexpr int bits = kDigitBits, half = 1 << (bits - 1);
+  U H = 0;
+#pragma unroll
+  for (int pos = 0; pos < NS - 1; ++pos) H |= (U)half << (bits * pos);
+  const unsigned long long ab = abs_bits(v);
   const unsigned long long frac = ab & ((1ull << 52) - 1);
   const int be = (int)(ab >> 52);
   const unsigned long long M = be ? (frac | (1ull << 52)) : frac;
   const int E = be ? be - 1075 : -1074;  // |v| = M * 2^E
-  const int sh = E - e + bits * slices;
+  const int sh = E - e + bits * NS;
   U X;
-  if (sh >= 0) X = (U)M << sh;
+  if (e == INT32_MAX) X = 0;
+  else if (sh >= 0) X = (U)M << sh;
   else if (sh > -64) X = (U)((M >> (-sh)) + ((M >> (-sh - 1)) & 1ull));
   else X = 0;
-  const U mask = ((U)1 << bits) - 1, half = (U)1 << (bits - 1);
-  for (int t = slices - 1; t >= 1; --t) {
-    const U low = X & mask;
-    const int dt = (low >= half) ? (int)low - (1 << bits) : (int)low;
-    out[(int64_t)t * plane_elems] = __int2half_rn(neg ? -dt : dt);
-    X = (dt < 0) ? ((X + (U)(-dt)) >> bits) : ((X - (U)dt) >> bits);
-  }
-  out[0] = __int2half_rn(neg ? -(int)X : (int)X);
+  return X + H;
 }
 
+// Digit planes of an operand for NS slices: plane t holds digit position
+// NS-1-t of every element (plane 0 the top digit), sign applied, as fp16.
+// A pair of digits d0, d1 in [-128, 128] becomes one __half2 without a
+// conversion instruction: the fp16 bit patterns 0x6400 + u are the integers
+// 1024 + u (u < 1024), so packing u = d + 128 under 0x6400 and subtracting
+// 1152 gives d exactly (and +0 for d = 0, as an integer conversion does).
+template <int NS>
 struct OzakiSliceOp {
   using Tout = __half;
+  using U = typename std::conditional<(kDigitBits * NS <= 62), unsigned long long, unsigned __int128>::type;
   const int* exps;
-  int slices;
-  int bits;
-  __device__ __forceinline__ void operator()(double v, int64_t r, __half* out, int64_t plane_elems) const {
+  __device__ __forceinline__ void pair(double v0, double v1, int64_t r, __half* out, int64_t plane_elems) const {
+    constexpr int bits = kDigitBits, half = 1 << (bits - 1);
+    constexpr unsigned mask = (1u << bits) - 1u;
     const int e = exps[r];
-    const unsigned long long ab = abs_bits(v);
-    const bool neg = __double_as_longlong(v) < 0;
-    if (e == INT32_MAX || ab == 0) {
-      for (int t = 0; t < slices; ++t) out[(int64_t)t * plane_elems] = __int2half_rn(0);
-    } else if (bits * slices <= 62) {
-      write_digits<unsigned long long>(ab, neg, e, bits, slices, out, plane_elems);
-    } else {
-      write_digits<unsigned __int128>(ab, neg, e, bits, slices, out, plane_elems);
+    const U Y0 = offset_digits<NS, U>(v0, e), Y1 = offset_digits<NS, U>(v1, e);
+    const bool n0 = __double_as_longlong(v0) < 0, n1 = __double_as_longlong(v1) < 0;
+    const __half2 bias = __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480));  // 1152
+    // least significant position first, into the last plane, walking back
+    U y0 = Y0, y1 = Y1;
+    __half* o = out + (int64_t)(NS - 1) * plane_elems;
+#pragma unroll
+    for (int pos = 0; pos < NS; ++pos) {
+      int d0, d1;
+      if (pos == NS - 1) {  // top digit: the remaining bits
+        d0 = (int)(unsigned)y0;
+        d1 = (int)(unsigned)y1;
+      } else {
+        d0 = (int)((unsigned)y0 & mask) - half;
+        d1 = (int)((unsigned)y1 & mask) - half;
+        y0 >>= bits;
+        y1 >>= bits;
+      }
+      const unsigned u0 = (unsigned)((n0 ? -d0 : d0) + 128), u1 = (unsigned)((n1 ? -d1 : d1) + 128);
+      const unsigned w = 0x64006400u | u0 | (u1 << 16);
+      *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
+      o -= plane_elems;
     }
   }
 };
 
+template <int NS>
+void launch_ozaki_planes(const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, __half* planes, int64_t ldp,
+                         int64_t plane_elems, const int* exps, cudaStream_t s) {
+  planes::launch_to_planes(x, sr, sp, R, K, planes, ldp, plane_elems, OzakiSliceOp<NS>{exps}, s);
+}
+
+// Runtime slice count -> the unrolled kernel for it (1..16).
+void ozaki_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, __half* planes, int64_t ldp,
+                  int64_t plane_elems, const int* exps, cudaStream_t s) {
+  switch (ns) {
+#define MOMMS_OZAKI_NS(N) \
+  case N: launch_ozaki_planes<N>(x, sr, sp, R, K, planes, ldp, plane_elems, exps, s); break;
+    MOMMS_OZAKI_NS(1) MOMMS_OZAKI_NS(2) MOMMS_OZAKI_NS(3) MOMMS_OZAKI_NS(4) MOMMS_OZAKI_NS(5) MOMMS_OZAKI_NS(6)
+    MOMMS_OZAKI_NS(7) MOMMS_OZAKI_NS(8) MOMMS_OZAKI_NS(9) MOMMS_OZAKI_NS(10) MOMMS_OZAKI_NS(11) MOMMS_OZAKI_NS(12)
+    MOMMS_OZAKI_NS(13) MOMMS_OZAKI_NS(14) MOMMS_OZAKI_NS(15) MOMMS_OZAKI_NS(16)
+#undef MOMMS_OZAKI_NS
+    default: break;
+  }
+}
+
 // Sampled quantities for the slice-count bound: for sampled (i, j),
 //   q1 = (2^e_i sum|b_.j| + 2^f_j sum|a_i.|) / (|A||B|)_ij
-//   q2 = k 2^(e_i+f_j) / (|A||B|)_ij
-// reduced to their maxima in out[0], out[1] (as ordered non-negative floats).
-// Block (r, c) samples 32 consecutive rows of A against one column of B:
-// lanes walk the rows (coalesced for column-major A), warps split k.
-constexpr int kSampleRowBlocks = 8, kSampleCols = 8;
-__global__ void __launch_bounds__(256) sample_bound_kernel(const double* __restrict__ a, int64_t rsa, int64_t csa,
-                                                           const double* __restrict__ b, int64_t rsb, int64_t csb,
-                                                           int64_t m, int64_t n, int64_t k,
-                                                           const int* __restrict__ rexp, const int* __restrict__ cexp,
-                                                           unsigned long long* out) {
-  __shared__ double s_ab[8][32], s_a[8][32], s_b[8];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(blockIdx.x * 131 + blockIdx.y * 7 + 1);
+//      = (sum b' + sum a') / sum a'b'
+//   q2 = k 2^(e_i+f_j) / (|A||B|)_ij = k / sum a'b'
+// with a' = |a| 2^-e_i and b' = |b| 2^-f_j in [0, 1), reduced to their maxima
+// in out[0], out[1] (as ordered non-negative floats). The scaled magnitudes
+// are built from the exponent bits as FP32 (mantissa truncated, below 2^-126
+// flushed: an estimate needs no more), so the sums run on the FP32 pipe
+// rather than GB300's narrow FP64 one.
+// Sample (x, y) is 32 consecutive rows of A against one column of B, at
+// hashed positions. The sums run in two steps so that the work spreads over
+// the GPU and the result does not depend on timing: sample_partial_kernel
+// block (x, y, z) sums k range z (lanes walk the rows, coalesced for
+// column-major A; warps split the range) into its own slot, and
+// sample_final_kernel adds the slots in a fixed order.
+constexpr int kSampleRowBlocks = 8, kSampleCols = 8, kSamples = kSampleRowBlocks * kSampleCols;
+constexpr int kSampleSlot = 2 * 32 + 1;  // sab[32], sa[32], sb
+
+__device__ __forceinline__ void sample_position(int x, int y, int64_t m, int64_t n, int64_t* i0, int64_t* j) {
+  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(x * 131 + y * 7 + 1);
   h ^= h >> 31;
   h *= 0xBF58476D1CE4E5B9ull;
   h ^= h >> 29;
-  const int64_t i0 = m > 32 ? (int64_t)(h % (uint64_t)(m - 31)) : 0;
-  const int64_t j = (int64_t)((h >> 24) % (uint64_t)n);
+  *i0 = m > 32 ? (int64_t)(h % (uint64_t)(m - 31)) : 0;
+  *j = (int64_t)((h >> 24) % (uint64_t)n);
+}
+
+// |v| * 2^-e as FP32 from the bit pattern (|v| < 2^e, so at most just below 1).
+__device__ __forceinline__ float scaled_abs(double v, int e) {
+  const unsigned long long ab = abs_bits(v);
+  const int be = (int)(ab >> 52);
+  const int fe = be - 1023 - e + 127;
+  if (e == INT32_MAX || be == 0 || fe <= 0) return 0.0f;
+  return __uint_as_float(((unsigned)fe << 23) | (unsigned)((ab >> 29) & 0x7fffffull));
+}
+
+__global__ void __launch_bounds__(256) sample_partial_kernel(const double* __restrict__ a, int64_t rsa, int64_t csa,
+                                                             const double* __restrict__ b, int64_t rsb, int64_t csb,
+                                                             int64_t m, int64_t n, int64_t k, int64_t kc,
+                                                             const int* __restrict__ rexp,
+                                                             const int* __restrict__ cexp, double* __restrict__ part) {
+  __shared__ double s_ab[8][32], s_a[8][32], s_b[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t i0, j;
+  sample_position(blockIdx.x, blockIdx.y, m, n, &i0, &j);
   const int64_t i = i0 + lane;
-  double sab = 0.0, sa = 0.0, sb = 0.0;
-  for (int64_t pp = warp; pp < k; pp += 8) {
-    const double bv = fabs(b[pp * rsb + j * csb]);
+  const int ei = i < m ? rexp[i] : 0, fj = cexp[j];
+  const int64_t k0 = (int64_t)blockIdx.z * kc, k1 = min(k, k0 + kc);
+  float sab = 0.0f, sa = 0.0f, sb = 0.0f;
+  for (int64_t pp = k0 + warp; pp < k1; pp += 8) {
+    const float bv = scaled_abs(b[pp * rsb + j * csb], fj);
     sb += bv;
     if (i < m) {
-      const double av = fabs(a[i * rsa + pp * csa]);
-      sab += av * bv;
+      const float av = scaled_abs(a[i * rsa + pp * csa], ei);
+      sab = fmaf(av, bv, sab);
       sa += av;
     }
   }
@@ -183,21 +256,47 @@ __global__ void __launch_bounds__(256) sample_bound_kernel(const double* __restr
   s_a[warp][lane] = sa;
   if (lane == 0) s_b[warp] = sb;
   __syncthreads();
-  if (warp == 0 && i < m) {
-    for (int w = 1; w < 8; ++w) {
-      sab += s_ab[w][lane];
-      sa += s_a[w][lane];
+  if (warp == 0) {
+    double tab = 0.0, ta = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      tab += s_ab[w][lane];
+      ta += s_a[w][lane];
     }
-    sb = 0.0;
-    for (int w = 0; w < 8; ++w) sb += s_b[w];
-    const int ei = rexp[i], fj = cexp[j];
-    if (ei == INT32_MAX || fj == INT32_MAX || sab == 0.0) return;
-    const double q1 = (ldexp(sb, ei) + ldexp(sa, fj)) / sab;
-    const double q2 = ldexp((double)k, ei + fj) / sab;
-    // non-negative doubles order like their bit patterns
-    atomicMax(&out[0], (unsigned long long)__double_as_longlong(q1));
-    atomicMax(&out[1], (unsigned long long)__double_as_longlong(q2));
+    double* slot = part + ((int64_t)blockIdx.z * kSamples + blockIdx.y * kSampleRowBlocks + blockIdx.x) * kSampleSlot;
+    slot[lane] = tab;
+    slot[32 + lane] = ta;
+    if (lane == 0) {
+      double t = 0.0;
+      for (int w = 0; w < 8; ++w) t += s_b[w];
+      slot[64] = t;
+    }
   }
+}
+
+// One warp per sample: adds the k-range slots in order, then the maxima.
+__global__ void __launch_bounds__(32) sample_final_kernel(const double* __restrict__ part, int nz, int64_t m,
+                                                          int64_t n, int64_t k, const int* __restrict__ rexp,
+                                                          const int* __restrict__ cexp, unsigned long long* out) {
+  const int lane = threadIdx.x;
+  const int x = blockIdx.x % kSampleRowBlocks, y = blockIdx.x / kSampleRowBlocks;
+  int64_t i0, j;
+  sample_position(x, y, m, n, &i0, &j);
+  const int64_t i = i0 + lane;
+  double sab = 0.0, sa = 0.0, sb = 0.0;
+  for (int z = 0; z < nz; ++z) {
+    const double* slot = part + ((int64_t)z * kSamples + blockIdx.x) * kSampleSlot;
+    sab += slot[lane];
+    sa += slot[32 + lane];
+    sb += slot[64];
+  }
+  if (i >= m) return;
+  const int ei = rexp[i], fj = cexp[j];
+  if (ei == INT32_MAX || fj == INT32_MAX || sab == 0.0) return;
+  const double q1 = (sb + sa) / sab;
+  const double q2 = (double)k / sab;
+  // non-negative doubles order like their bit patterns
+  atomicMax(&out[0], (unsigned long long)__double_as_longlong(q1));
+  atomicMax(&out[1], (unsigned long long)__double_as_longlong(q2));
 }
 
 // Recombination of the exact group sums. Group g holds S_g = the int32 sum of
@@ -210,18 +309,25 @@ __global__ void __launch_bounds__(256) sample_bound_kernel(const double* __restr
 struct CombineParams {
   const int* sbuf;
   int64_t plane;
-  int ngroups;
-  int dmax;                     // min(largest d_g - 2, 12): R stays below 2^127; lower
-                                // diagonals lose bits beyond 2^(-12 bits) of the top one
-  uint8_t dgrp[sp::MAX_GROUPS];  // d_g - 2 per group
-  int64_t m, n;
+  // Horner over the levels L = d_g - 2 <= dmax: entry q multiplies R by
+  // 2^(bits * hsh[q]) and then adds group hg[q]'s S_g (hg[q] == 255: none).
+  // Groups below dmax (lower diagonals; dmax = min(largest level, 12) keeps R below
+  // 2^127) are added as S_g >> tail_sh.
+  int nh;
+  uint8_t hg[2 * sp::MAX_GROUPS];
+  uint8_t hsh[2 * sp::MAX_GROUPS];  // 0 or 1
+  int ntail;
+  uint8_t tail_g[sp::MAX_GROUPS];
+  uint8_t tail_sh[sp::MAX_GROUPS];
+  int scale_off;  // -2 bits - bits*dmax
+  int alpha_one, beta_zero;
+  int64_t m;
+  int64_t j0, j1;  // columns of C this launch finishes
   const int* row_exp;
   const int* col_exp;
-  int bits;
   double alpha, beta;
   double* c;
   int64_t rsc, csc;
-  int64_t e_begin, e_end;  // entries [e_begin, e_end) of C in column order (e = i + j*m)
 };
 
 // Nearest double to a 128-bit signed integer times 2^scale.
@@ -240,27 +346,105 @@ __device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
     const unsigned __int128 rest = U & (((unsigned __int128)1 << sh) - 1);
     if (rest != 0) top |= 1ull;  // sticky bit: top keeps 64 significant bits
   }
-  const double v = __ull2double_rn(top);  // the only rounding
-  return ldexp(neg ? -v : v, sh + scale);
+  // Round top to 53 significant bits (nearest, ties to even) and place the
+  // exponent directly: integer instructions only, since GB300's FP64 pipe is
+  // narrow. Same result as converting top to double (the only rounding) and
+  // scaling by 2^(sh + scale) exactly, which is what the rare results outside
+  // the normal range still do.
+  const int lz = __clzll((long long)top);
+  const unsigned long long t = top << lz;  // bit 63 set
+  unsigned long long mant = t >> 11;
+  const unsigned rb = (unsigned)(t & 0x7ffull);
+  if (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ++mant;
+  int E = 63 - lz + sh + scale;  // value = (mant / 2^52) * 2^E
+  if (mant >> 53) {
+    mant >>= 1;
+    ++E;
+  }
+  if (E < -1022 || E > 1023) {
+    const double v = __ull2double_rn(top);
+    return ldexp(neg ? -v : v, sh + scale);
+  }
+  const unsigned long long b = ((unsigned long long)(E + 1023) << 52) | (mant & ((1ull << 52) - 1)) |
+                               (neg ? (1ull << 63) : 0ull);
+  return __longlong_as_double((long long)b);
 }
 
+// Thread rows i and i + 256 of block row blockIdx.x, for columns
+// j0 + blockIdx.y, stepping by gridDim.y: no index division, the row
+// exponents stay in registers, and the two rows' loads are in flight together.
+constexpr int kCombineBatch = 16;  // Horner entries whose loads are issued together
+
 __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
-  for (int64_t e = p.e_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < p.e_end;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e % p.m, j = e / p.m;
-    __int128 R = 0;
-    for (int g = 0; g < p.ngroups; ++g) {
-      const int sh = p.bits * (p.dmax - p.dgrp[g]);
-      const __int128 Sg = (__int128)p.sbuf[g * p.plane + e];
-      R += sh >= 0 ? (Sg << sh) : (Sg >> (-sh));
+  constexpr int bits = kDigitBits;
+  using u128 = unsigned __int128;
+  int64_t rows[2];
+  int er[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    rows[u] = (int64_t)blockIdx.x * 512 + threadIdx.x + 256 * u;
+    er[u] = rows[u] < p.m ? p.row_exp[rows[u]] : 0;
+  }
+  if (rows[0] >= p.m) return;
+  const bool two = rows[1] < p.m;
+  for (int64_t j = p.j0 + blockIdx.y; j < p.j1; j += gridDim.y) {
+    const int ec = p.col_exp[j];
+    const int* col = p.sbuf + j * p.m;
+    // two's complement in unsigned 128-bit arithmetic
+    u128 R0 = 0, R1 = 0;
+    if (p.nh <= kCombineBatch) {
+      // all loads first (up to 2 x kCombineBatch in flight), then the Horner steps
+      int s0[kCombineBatch], s1[kCombineBatch];
+#pragma unroll
+      for (int q = 0; q < kCombineBatch; ++q) {
+        s0[q] = 0;
+        s1[q] = 0;
+        if (q < p.nh && p.hg[q] != 255) {
+          const int* sg = col + (int64_t)p.hg[q] * p.plane;
+          s0[q] = sg[rows[0]];
+          if (two) s1[q] = sg[rows[1]];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kCombineBatch; ++q) {
+        if (q < p.nh) {
+          if (p.hsh[q]) {  // next level: one constant shift
+            R0 <<= bits;
+            R1 <<= bits;
+          }
+          R0 += (u128)(__int128)s0[q];
+          R1 += (u128)(__int128)s1[q];
+        }
+      }
+    } else {
+      for (int q = 0; q < p.nh; ++q) {
+        if (p.hsh[q]) {
+          R0 <<= bits;
+          R1 <<= bits;
+        }
+        const int g = p.hg[q];
+        if (g != 255) {
+          const int* sg = col + (int64_t)g * p.plane;
+          R0 += (u128)(__int128)sg[rows[0]];
+          if (two) R1 += (u128)(__int128)sg[rows[1]];
+        }
+      }
     }
-    const int er = p.row_exp[i], ec = p.col_exp[j];
-    double v;
-    if (er == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-    else v = i128_to_double(R, er + ec - 2 * p.bits - p.bits * p.dmax);
-    double* cp = p.c + i * p.rsc + j * p.csc;
-    const double sv = v * p.alpha;
-    *cp = (p.beta == 0.0) ? sv : fma(p.beta, *cp, sv);
+    for (int q = 0; q < p.ntail; ++q) {
+      const int* sg = col + (int64_t)p.tail_g[q] * p.plane;
+      R0 += (u128)(__int128)(sg[rows[0]] >> p.tail_sh[q]);
+      if (two) R1 += (u128)(__int128)(sg[rows[1]] >> p.tail_sh[q]);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 && !two) break;
+      double v;
+      if (er[u] == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
+      else v = i128_to_double((__int128)(u == 0 ? R0 : R1), er[u] + ec + p.scale_off);
+      double* cp = p.c + rows[u] * p.rsc + j * p.csc;
+      const double sv = p.alpha_one ? v : v * p.alpha;  // v * 1 == v: one FP64 operation saved
+      *cp = p.beta_zero ? sv : fma(p.beta, *cp, sv);
+    }
   }
 }
 
@@ -294,14 +478,20 @@ int compute_exponents(const DevGemm& g, unsigned long long* maxbits, int* exps, 
 int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double target, int bits, cudaStream_t s,
                   int* ns_out, double* bound_out) {
   const double tgt = target > 0.0 ? target : ldexp(1.0, -52);
+  // k ranges of at least 512 per block, at most 32 ranges
+  const int nz = (int)std::max<int64_t>(1, std::min<int64_t>(32, g.k / 512));
+  const int64_t kc = ceil_div(g.k, nz);
   unsigned long long* q = nullptr;
-  cudaError_t ce = scratch_alloc(&q, 2 * sizeof(unsigned long long), s);
+  const size_t part_bytes = (size_t)nz * kSamples * kSampleSlot * sizeof(double);
+  cudaError_t ce = scratch_alloc(&q, 2 * sizeof(unsigned long long) + part_bytes, s);
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound sample");
+  double* part = reinterpret_cast<double*>(q + 2);
   cudaMemsetAsync(q, 0, 2 * sizeof(unsigned long long), s);
-  sample_bound_kernel<<<dim3(kSampleRowBlocks, kSampleCols), 256, 0, s>>>(
+  sample_partial_kernel<<<dim3(kSampleRowBlocks, kSampleCols, nz), 256, 0, s>>>(
       static_cast<const double*>(g.a.ptr), g.a.rs, g.a.cs, static_cast<const double*>(g.b.ptr), g.b.rs, g.b.cs, g.m,
-      g.n, g.k, rexp, cexp, q);
-  note_launch();
+      g.n, g.k, kc, rexp, cexp, part);
+  sample_final_kernel<<<kSamples, 32, 0, s>>>(part, nz, g.m, g.n, g.k, rexp, cexp, q);
+  note_launch(2);
   unsigned long long hq[2] = {0, 0};
   ce = cudaMemcpyAsync(hq, q, sizeof(hq), cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
@@ -430,8 +620,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   __half* pb = planes_buf + (size_t)ns * a_plane;
   {
     KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    planes::launch_to_planes(A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, OzakiSliceOp{rexp, ns, bits}, s);
-    planes::launch_to_planes(B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, OzakiSliceOp{cexp, ns, bits}, s);
+    ozaki_planes(ns, A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, rexp, s);
+    ozaki_planes(ns, B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, cexp, s);
   }
   note_launch(2);
 
@@ -460,6 +650,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   p.tiles_n = (int)ceil_div(n, sp::BN);
   CombineParams cp;
   memset(&cp, 0, sizeof(cp));
+  uint8_t dgrp[sp::MAX_GROUPS];  // level (d - 2) of each group
   // Diagonals from the smallest weight (d = ns+1) to the largest (d = 2). A
   // diagonal whose int32 sums could pass 2^30 is split into several groups
   // of whole pairs; only the first group of a diagonal shifts R by 2^-bits.
@@ -485,7 +676,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       if (ng >= sp::MAX_GROUPS) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
       p.group_begin[ng] = np;
       p.chunk_kb[ng] = chunk;
-      cp.dgrp[ng] = (uint8_t)(d - 2);
+      dgrp[ng] = (uint8_t)(d - 2);
       for (int i = i0; i < std::min(nt, i0 + pairs_per_group); ++i) {
         p.pair_a[np] = (uint8_t)(tlist[i] - 1);
         p.pair_b[np] = (uint8_t)(d - tlist[i] - 1);
@@ -519,13 +710,41 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
 
   cp.sbuf = sbuf;
   cp.plane = (int64_t)plane;
-  cp.ngroups = ng;
-  cp.dmax = std::min(ns - 1, 12);
+  {
+    // Horner entries in level order: a shift by one level between levels
+    // (an empty level only shifts), then each group of the level
+    const int dmax = std::min(ns - 1, 12);
+    int nh = 0;
+    for (int L = 0; L <= dmax; ++L) {
+      bool first = true;
+      for (int gi = 0; gi < ng; ++gi)
+        if (dgrp[gi] == L) {
+          cp.hg[nh] = (uint8_t)gi;
+          cp.hsh[nh] = (uint8_t)((first && L > 0) ? 1 : 0);
+          ++nh;
+          first = false;
+        }
+      if (first && L > 0) {  // no group at this level
+        cp.hg[nh] = 255;
+        cp.hsh[nh] = 1;
+        ++nh;
+      }
+    }
+    cp.nh = nh;
+    cp.ntail = 0;
+    for (int gi = 0; gi < ng; ++gi)
+      if (dgrp[gi] > dmax) {
+        cp.tail_g[cp.ntail] = (uint8_t)gi;
+        cp.tail_sh[cp.ntail] = (uint8_t)(bits * (dgrp[gi] - dmax));
+        ++cp.ntail;
+      }
+    cp.scale_off = -2 * bits - bits * dmax;
+    cp.alpha_one = (g.alpha == 1.0);
+    cp.beta_zero = (g.beta == 0.0);
+  }
   cp.m = m;
-  cp.n = n;
   cp.row_exp = rexp;
   cp.col_exp = cexp;
-  cp.bits = bits;
   cp.alpha = g.alpha;
   cp.beta = g.beta;
   cp.c = static_cast<double*>(g.c.ptr);
@@ -537,12 +756,13 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int64_t nchunks = (g.staging && g.staging->writeback) ? std::min<int64_t>(4, n) : 1;
   for (int64_t ch = 0; ch < nchunks; ++ch) {
     const int64_t j0 = n * ch / nchunks, j1 = n * (ch + 1) / nchunks;
-    cp.e_begin = j0 * m;
-    cp.e_end = j1 * m;
-    const int cblocks = (int)std::min<int64_t>(ceil_div(cp.e_end - cp.e_begin, 256), (int64_t)ds->sm_count * 16);
+    cp.j0 = j0;
+    cp.j1 = j1;
+    const int64_t bx = ceil_div(m, 512);
+    const int64_t by = std::min<int64_t>({j1 - j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
     {
       KernelTimer kt(MOMMS_KERNEL_COMBINE, s);
-      combine_kernel<<<cblocks, 256, 0, s>>>(cp);
+      combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, s>>>(cp);
     }
     note_launch();
     ce = cudaGetLastError();

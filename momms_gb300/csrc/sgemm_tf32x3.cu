@@ -16,13 +16,21 @@ namespace momms {
 namespace {
 struct Tf32SplitOp {
   using Tout = float;
-  __device__ __forceinline__ void operator()(float v, int64_t, float* out, int64_t plane_elems) const {
+  __device__ __forceinline__ static void split(float v, float* hi_out, float* lo_out) {
     uint32_t hi, lo;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(v));
     const float rest = v - __uint_as_float(hi);
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(rest));
-    out[0] = __uint_as_float(hi);
-    out[plane_elems] = __uint_as_float(lo);
+    *hi_out = __uint_as_float(hi);
+    *lo_out = __uint_as_float(lo);
+  }
+  // two neighbouring elements of a row: one 8-byte store per plane
+  __device__ __forceinline__ void pair(float v0, float v1, int64_t, float* out, int64_t plane_elems) const {
+    float2 hi, lo;
+    split(v0, &hi.x, &lo.x);
+    split(v1, &hi.y, &lo.y);
+    *reinterpret_cast<float2*>(out) = hi;
+    *reinterpret_cast<float2*>(out + plane_elems) = lo;
   }
 };
 }  // namespace
