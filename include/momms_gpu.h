@@ -254,7 +254,7 @@ typedef struct {
   int32_t pairs;          /* OZAKI: slice products formed (tensor-core GEMMs) */
   int32_t groups;         /* OZAKI: accumulation groups */
   int32_t splits;         /* plain paths: k splits */
-  int32_t reserved;
+  int32_t multicast;      /* tensor-core paths: 1 if the slice kernel ran as clusters of two CTAs sharing B tiles */
   double bound_rel_err;   /* OZAKI: predicted worst-case |dC|/(|A||B|) */
 } momms_call_info;
 int momms_last_info(momms_call_info* out);

@@ -1,10 +1,10 @@
 """momms_gb300: the GB300 (sm_103a) blocked matrix multiply C := beta*C + alpha*A*B.
 
 The product is the shared library ``libmomms_gpu.so`` built from ``csrc/``;
-its C ABI is ``include/momms_gpu.h``. This package loads that library and
-gives Python callers the same view-based interface the reference exposes
-(``momms_gb300.matrix.Matrix`` and the ``GemmNode`` family in
-``momms_gb300.nodes``). There is no CPU fallback: if the library is missing,
+its C ABI is ``include/momms_gpu.h`` and the reference's view-based
+``GemmNode`` interface over it is ``include/momms/gemm_node.hpp`` (C++). This
+package loads the library for Python callers through ctypes, with the C
+structs mirrored below. There is no CPU fallback: if the library is missing,
 loading it raises.
 """
 import ctypes
@@ -58,7 +58,7 @@ class GemmDesc(ctypes.Structure):
 
 class CallInfo(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("slices", ctypes.c_int32), ("pairs", ctypes.c_int32),
-                ("groups", ctypes.c_int32), ("splits", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("groups", ctypes.c_int32), ("splits", ctypes.c_int32), ("multicast", ctypes.c_int32),
                 ("bound_rel_err", ctypes.c_double)]
 
 

@@ -512,8 +512,7 @@ int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double tar
 }  // namespace
 
 int set_attrs_ozaki() {
-  cudaError_t e = cudaFuncSetAttribute(sp::slice_gemm_kernel<0, sp::EPI_OZAKI>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  cudaError_t e = sp::set_slice_attrs<0, sp::EPI_OZAKI>();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(Ozaki)");
 }
 
@@ -626,17 +625,21 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   note_launch(2);
 
   if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 per launch");
-  CUtensorMap tmA, tmB;
+  CUtensorMap tmA, tmB, tmB_half;
   {
     uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)ns};
     uint64_t strides[2] = {(uint64_t)kp * 2, (uint64_t)a_plane * 2};
-    uint32_t box[3] = {64, (uint32_t)sp::BM, 1};
+    uint32_t box[3] = {64, (uint32_t)sp::BM, 1};  // 128-byte k-blocks
     int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
     uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)ns};
     uint64_t stridesb[2] = {(uint64_t)kp * 2, (uint64_t)b_plane * 2};
     uint32_t boxb[3] = {64, (uint32_t)sp::BN, 1};
     rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
+    rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb, dimsb, stridesb, boxh,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
   }
 
@@ -668,9 +671,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     }
     // every TMEM chunk keeps |sum| <= 2^22 (exact in FP32, and inside the
     // magic-constant conversion range)
-    const int chunk = (int)std::max<int64_t>(1, (int64_t)(ldexp(1.0, 22) / maxprod) / 64);
+    const int chunk = (int)std::max<int64_t>(1, (int64_t)(ldexp(1.0, 22) / maxprod) / p.kelems);
     // pairs per group so that the int32 group sums stay below 2^30
-    const double per_pair = (double)p.kblocks * 64.0 * maxprod;
+    const double per_pair = (double)p.kblocks * p.kelems * maxprod;
     const int pairs_per_group = (int)std::max(1.0, floor(ldexp(1.0, 30) / per_pair));
     for (int i0 = 0; i0 < nt; i0 += pairs_per_group) {
       if (ng >= sp::MAX_GROUPS) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
@@ -699,12 +702,12 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   p.plane = (int64_t)plane;
   p.status = ds->status;
 
-  auto kern = sp::slice_gemm_kernel<0, sp::EPI_OZAKI>;
-  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
-  const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
   {
     KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, s);
-    kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+    bool mc = false;
+    ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, s, &mc);
+    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki slice launch");
+    call_info().multicast = mc ? 1 : 0;
   }
   note_launch();
 

@@ -36,8 +36,7 @@ struct Tf32SplitOp {
 }  // namespace
 
 int set_attrs_tf32() {
-  cudaError_t e = cudaFuncSetAttribute(sp::slice_gemm_kernel<1, sp::EPI_F32>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sp::SMEM_BYTES);
+  cudaError_t e = sp::set_slice_attrs<1, sp::EPI_F32>();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(split-TF32)");
 }
 
@@ -66,17 +65,21 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   }
   note_launch(2);
 
-  CUtensorMap tmA, tmB;
+  CUtensorMap tmA, tmB, tmB_half;
   {
     uint64_t dims[3] = {(uint64_t)g.k, (uint64_t)g.m, 2};
     uint64_t strides[2] = {(uint64_t)kp * 4, (uint64_t)a_plane * 4};
-    uint32_t box[3] = {32, (uint32_t)sp::BM, 1};
+    uint32_t box[3] = {32, (uint32_t)sp::BM, 1};  // 128-byte k-blocks
     int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
     uint64_t dimsb[3] = {(uint64_t)g.k, (uint64_t)g.n, 2};
     uint64_t stridesb[2] = {(uint64_t)kp * 4, (uint64_t)b_plane * 4};
     uint32_t boxb[3] = {32, (uint32_t)sp::BN, 1};
     rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    uint32_t boxh[3] = {32, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
+    rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pb, dimsb, stridesb, boxh,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
   }
 
@@ -105,12 +108,12 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
 
   // the epilogue reads C
   if ((ce = wait_operand(g, 2, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
-  auto kern = sp::slice_gemm_kernel<1, sp::EPI_F32>;
-  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
-  const int grid = (int)std::min<int64_t>(tiles, ds->sm_count);
   {
     KernelTimer kt(MOMMS_KERNEL_SLICE_TF32, s);
-    kern<<<grid, sp::THREADS, sp::SMEM_BYTES, s>>>(tmA, tmB, p);
+    bool mc = false;
+    ce = sp::launch_slice<1, sp::EPI_F32>(tmA, tmB, tmB_half, p, ds->sm_count, s, &mc);
+    if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 slice launch");
+    call_info().multicast = mc ? 1 : 0;
   }
   note_launch();
   ce = cudaGetLastError();

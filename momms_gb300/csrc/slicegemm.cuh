@@ -12,6 +12,15 @@
 // memory descriptors expect. Warp roles: warp 0 issues TMA, warp 1 (one
 // thread) issues tcgen05.mma and commits, warps 2..9 drain TMEM.
 //
+// Multicast variant (MC): CTAs run in clusters of two on vertically adjacent
+// output tiles (tm = 2 * pair + rank, same tn), which read the same B tile.
+// Each CTA loads its own A tile and one half of the B tile, multicast into
+// both CTAs' shared memory, so a stage costs each SM two thirds of the L2
+// reads; each CTA's MMA thread releases a stage in both CTAs
+// (empty barriers count two arrivals), since the peer's next multicast
+// writes into it. A cluster barrier after initialisation and before exit
+// keeps every remote write and arrival inside the lifetime of its target.
+//
 // Two epilogues:
 //   EPI_F32   : one group; finished chunks are summed in FP32 registers
 //               (round to nearest) and C = alpha*sum + beta*C is written at
@@ -23,6 +32,10 @@
 //               recombination runs afterwards in its own kernel, so no FP64
 //               work sits in this pipeline).
 #pragma once
+#include <stdlib.h>
+
+#include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "tc_common.cuh"
@@ -30,9 +43,15 @@
 namespace momms {
 namespace sp {
 
+// A stage holds one k-block of each operand: 128 bytes of k per row (64 fp16
+// or 32 fp32 elements) in the 128-byte swizzle. (64-byte k-blocks with the
+// 64-byte swizzle fit nine stages instead of four but measured 25 % slower:
+// twice the TMA row requests per byte.)
 constexpr int BM = 128, BN = 256, STAGES = 4;
-constexpr int A_TILE = BM * 128;  // bytes: 128 rows x 128-byte k-block
-constexpr int B_TILE = BN * 128;
+constexpr int ROW_BYTES = 128;
+constexpr int KSTEPS = ROW_BYTES / 32;  // MMAs per stage (each consumes 32 bytes of k)
+constexpr int A_TILE = BM * ROW_BYTES;
+constexpr int B_TILE = BN * ROW_BYTES;
 constexpr int STAGE_BYTES = A_TILE + B_TILE;  // 48 KB
 constexpr int EPI_WARPS = 8;                     // 2 per TMEM lane quarter
 constexpr int EPI_COLS = BN / (EPI_WARPS / 4);   // columns drained per thread
@@ -46,7 +65,7 @@ enum { EPI_F32 = 0, EPI_OZAKI = 1 };
 struct Params {
   int64_t m, n;
   int kblocks;  // k-blocks per plane
-  int kelems;   // elements per k-block (64 for f16, 32 for tf32)
+  int kelems;   // elements per k-block (64 for f16, 32 for tf32: 128 bytes)
   int tiles_m, tiles_n;
   int ngroups;
   int group_begin[MAX_GROUPS + 1];
@@ -68,8 +87,8 @@ __device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0;
 // so that the ~152 tiles in flight at once share 16 A row panels and about
 // 10 B column panels of each slice plane in L2 (a plain column-major sweep
 // would touch a whole 128 MB plane per pair at m = 8192).
+template <int G>
 __device__ __forceinline__ void tile_coords(int64_t t, int tiles_m, int tiles_n, int& tm, int& tn) {
-  constexpr int G = 16;
   const int64_t per_group = (int64_t)G * tiles_n;
   const int64_t g = t / per_group, r = t % per_group;
   const int first = (int)(g * G);
@@ -84,7 +103,7 @@ __device__ __forceinline__ int f2i_exact(uint32_t bits) {
   return (int)(__float_as_uint(f) - 0x4B400000u);
 }
 
-template <int KIND, int EPI>
+template <int KIND, int EPI, bool MC>
 __global__ void __launch_bounds__(THREADS, 1)
     slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ Params p) {
@@ -99,10 +118,22 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // work units: output tiles, or (MC) vertical tile pairs, one per cluster
+  const uint32_t rank = MC ? cluster_ctarank() : 0u;
+  const int64_t unit0 = MC ? (int64_t)cluster_id_x() : (int64_t)blockIdx.x;
+  const int64_t unit_step = MC ? (int64_t)cluster_count_x() : (int64_t)gridDim.x;
+  const int units_m = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  const int64_t units = (int64_t)units_m * p.tiles_n;
+  auto coords = [&](int64_t t, int& tm, int& tn) {
+    int um;
+    tile_coords<MC ? 8 : 16>(t, units_m, p.tiles_n, um, tn);
+    tm = MC ? 2 * um + (int)rank : um;  // MC: rank 1 of an odd last pair reads zero rows, writes nothing
+  };
+
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&empty[i], 1);
+      mbar_init(&empty[i], MC ? 2 : 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
@@ -118,10 +149,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   tc::fence_before();
   __syncthreads();
+  if (MC) cluster_sync();  // the peer's barriers exist before any multicast reaches them
   tc::fence_after();
   const uint32_t tmem_base = *tmem_slot;
-
-  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
 
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
@@ -132,9 +162,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       uint32_t armed = 0;  // bit s: stage s has been armed at least once
       uint32_t last_ph = 0;  // bit s: parity of the phase last armed on stage s
-      for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
         int tm, tn;
-        tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+        coords(t, tm, tn);
         for (int g = 0; g < p.ngroups; ++g) {
           for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
             for (int kb = 0; kb < p.kblocks; ++kb) {
@@ -151,12 +181,31 @@ __global__ void __launch_bounds__(THREADS, 1)
               mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
               uint8_t* sa = smem + stage * STAGE_BYTES;
               tma_load_3d(sa, &tmA, &full[stage], kb * p.kelems, tm * BM, p.pair_a[pi]);
-              tma_load_3d(sa + A_TILE, &tmB, &full[stage], kb * p.kelems, tn * BN, p.pair_b[pi]);
+              if (MC)  // this CTA's half of the B tile, into both CTAs (its tmB box is BN/2 rows)
+                tma_load_3d_mc(sa + A_TILE + rank * (B_TILE / 2), &tmB, &full[stage], kb * p.kelems,
+                               tn * BN + (int)rank * (BN / 2), p.pair_b[pi], (uint16_t)0x3);
+              else
+                tma_load_3d(sa + A_TILE, &tmB, &full[stage], kb * p.kelems, tn * BN, p.pair_b[pi]);
               if (++stage == STAGES) {
                 stage = 0;
                 ph ^= 1;
               }
             }
+          }
+        }
+      }
+      if (MC && !aborted(abort_flag)) {
+        // every stage released by both CTAs: no arrival from the peer is
+        // still on its way to this CTA's barriers
+        for (int i = 0; i < STAGES; ++i) {
+          if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
+            report_status(p.status, DEV_TIMEOUT_EMPTY);
+            *abort_flag = 1;
+            break;
+          }
+          if (++stage == STAGES) {
+            stage = 0;
+            ph ^= 1;
           }
         }
       }
@@ -170,7 +219,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       int buf = 0;
       uint32_t acc_ph[2] = {0, 0};
-      for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
         for (int g = 0; g < p.ngroups; ++g) {
           const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
           const int chunk = p.chunk_kb[g];
@@ -193,10 +242,13 @@ __global__ void __launch_bounds__(THREADS, 1)
               const uint32_t a_addr = smem_u32(smem + stage * STAGE_BYTES);
               const uint32_t b_addr = a_addr + A_TILE;
 #pragma unroll
-              for (int kk = 0; kk < 4; ++kk)
+              for (int kk = 0; kk < KSTEPS; ++kk)
                 tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
                               (st > s0 || kk > 0) ? 1u : 0u);
-              tc::commit(&empty[stage]);
+              if (MC)
+                tc::commit_mc(&empty[stage], (uint16_t)0x3);  // both CTAs' copies of the stage are free
+              else
+                tc::commit(&empty[stage]);
               if (++stage == STAGES) {
                 stage = 0;
                 ph ^= 1;
@@ -223,9 +275,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int r_local = q * 32 + lane;
     int buf = 0;
     uint32_t acc_ph[2] = {0, 0};
-    for (int64_t t = blockIdx.x; t < tiles && !aborted(abort_flag); t += gridDim.x) {
+    for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
       int tm, tn;
-      tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+      coords(t, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
       // per-thread accumulators of finished chunks: exact int32 digit sums
@@ -298,10 +350,89 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncwarp();
   tc::fence_before();
   __syncthreads();
+  if (MC) cluster_sync();  // the peer is done writing into this CTA
   if (warp == 1) {
     tc::fence_after();
     tc::tmem_dealloc(tmem_base, TMEM_COLS);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+template <int KIND, int EPI>
+inline cudaError_t set_slice_attrs() {
+  cudaError_t e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SMEM_BYTES);
+  return e;
+}
+
+// Clusters of two of the multicast kernel that fit on the current device at
+// once (0: none, or multicast switched off by MOMMS_SLICE_MULTICAST=0).
+// Queried once per device.
+template <int KIND, int EPI>
+inline int slice_clusters() {
+  static std::atomic<int> cache[64];
+  static std::atomic<bool> init[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (init[dev].load()) return cache[dev].load();
+  int n = 0;
+  const char* env = getenv("MOMMS_SLICE_MULTICAST");
+  if (!(env && env[0] == '0')) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&n, (const void*)slice_gemm_kernel<KIND, EPI, true>, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      n = 0;
+    }
+  }
+  cache[dev].store(n);
+  init[dev].store(true);
+  return n;
+}
+
+// Launches the slice kernel: the multicast variant (clusters of two CTAs,
+// tmB_half's box is BN/2 rows) when the device takes clusters and there are
+// at least two m-tiles, otherwise one CTA per SM with tmB_full. Returns
+// whether the multicast variant ran in *mc.
+template <int KIND, int EPI>
+inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_full, const CUtensorMap& tmB_half,
+                                const Params& p, int sm_count, cudaStream_t s, bool* mc) {
+  const int clusters = p.tiles_m >= 2 ? slice_clusters<KIND, EPI>() : 0;
+  *mc = clusters > 0;
+  if (*mc) {
+    const int64_t units = (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, slice_gemm_kernel<KIND, EPI, true>, tmA, tmB_half, p);
+  }
+  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+  const int grid = (int)std::min<int64_t>(tiles, sm_count);
+  slice_gemm_kernel<KIND, EPI, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, p);
+  return cudaGetLastError();
 }
 
 }  // namespace sp

@@ -76,6 +76,16 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
                : "memory");
 }
 
+// Same, arriving on the mbarrier at `bar`'s offset in every CTA of the
+// cluster in `mask`.
+__device__ __forceinline__ void commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
 // ---- TMEM -> registers: 32 lanes x 32 consecutive 32-bit columns ----
 __device__ __forceinline__ void ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
