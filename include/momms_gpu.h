@@ -254,7 +254,8 @@ typedef struct {
   int32_t pairs;          /* OZAKI: slice products formed (tensor-core GEMMs) */
   int32_t groups;         /* OZAKI: accumulation groups */
   int32_t splits;         /* plain paths: k splits */
-  int32_t multicast;      /* tensor-core paths: 1 if the slice kernel ran as clusters of two CTAs sharing B tiles */
+  int32_t multicast;      /* tensor-core paths: slice kernel variant run: 0 = one CTA per tile, 1 = clusters
+                             of two sharing B tiles by multicast, 2 = CTA pairs with one cta_group::2 MMA */
   double bound_rel_err;   /* OZAKI: predicted worst-case |dC|/(|A||B|) */
 } momms_call_info;
 int momms_last_info(momms_call_info* out);

@@ -704,10 +704,10 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
 
   {
     KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, s);
-    bool mc = false;
-    ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, s, &mc);
+    int variant = 0;
+    ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, s, &variant);
     if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki slice launch");
-    call_info().multicast = mc ? 1 : 0;
+    call_info().multicast = variant;
   }
   note_launch();
 

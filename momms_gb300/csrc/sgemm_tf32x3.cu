@@ -110,10 +110,10 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   if ((ce = wait_operand(g, 2, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   {
     KernelTimer kt(MOMMS_KERNEL_SLICE_TF32, s);
-    bool mc = false;
-    ce = sp::launch_slice<1, sp::EPI_F32>(tmA, tmB, tmB_half, p, ds->sm_count, s, &mc);
+    int variant = 0;
+    ce = sp::launch_slice<1, sp::EPI_F32>(tmA, tmB, tmB_half, p, ds->sm_count, s, &variant);
     if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 slice launch");
-    call_info().multicast = mc ? 1 : 0;
+    call_info().multicast = variant;
   }
   note_launch();
   ce = cudaGetLastError();

@@ -358,6 +358,257 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// CTA-pair kernel (cta_group::2). A cluster of two CTAs computes a 256 x 256
+// output tile with one MMA stream: each CTA holds 128 rows of A and 128 rows
+// (columns of the output) of B per stage, and the even CTA issues
+// tcgen05.mma.cta_group::2, which reads both CTAs' shared memory and writes
+// 128 output rows into each CTA's TMEM. Against the single-CTA kernel this
+// reads two thirds of the shared-memory bytes per FLOP (the B half is read
+// once for both SMs) and a stage is 32 KB, so seven stages fit.
+//   full[s]   (even CTA)  both CTAs' TMA loads complete here (64 KB)
+//   empty[s]  (each CTA)  the even CTA's commit, multicast: stage s is free
+//   tfull[b]  (each CTA)  the even CTA's commit, multicast: accumulator b done
+//   tempty[b] (even CTA)  all 16 epilogue warps of the pair: b drained
+// ---------------------------------------------------------------------------
+constexpr int PSTAGES = 7;
+constexpr int P_STAGE_BYTES = A_TILE + B_TILE / 2;  // 32 KB
+constexpr int P_SMEM_BYTES = 1024 + PSTAGES * P_STAGE_BYTES + 256;
+
+template <int KIND, int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    slice_gemm_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
+                           const __grid_constant__ Params p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + PSTAGES * P_STAGE_BYTES);
+  uint64_t* empty = full + PSTAGES;
+  uint64_t* tfull = empty + PSTAGES;  // [2]
+  uint64_t* tempty = tfull + 2;       // [2]
+  uint64_t* drain = tempty + 2;       // used only when aborting
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_ctarank();
+  const bool leader = (rank == 0);
+  const int64_t unit0 = (int64_t)cluster_id_x(), unit_step = (int64_t)cluster_count_x();
+  const int units_m = (p.tiles_m + 1) / 2;
+  const int64_t units = (int64_t)units_m * p.tiles_n;
+  auto coords = [&](int64_t t, int& tm, int& tn) {
+    int um;
+    tile_coords<8>(t, units_m, p.tiles_n, um, tn);
+    tm = 2 * um + (int)rank;  // rank 1 of an odd last pair reads zero rows, writes nothing
+  };
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < PSTAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 2 * EPI_WARPS);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc2(tmem_slot, TMEM_COLS);
+    tc::tmem_relinquish2();
+  }
+  tc::fence_before();
+  __syncthreads();
+  cluster_sync();  // the pair's barriers exist before any remote arrival
+  tc::fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------ TMA producer (both CTAs) ------------------------------
+    if (lane == 0) {
+      prefetch_tensormap(&tmA);
+      prefetch_tensormap(&tmBh);
+      int stage = 0;
+      uint32_t ph = 0;
+      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+        int tm, tn;
+        coords(t, tm, tn);
+        for (int g = 0; g < p.ngroups; ++g) {
+          for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
+            for (int kb = 0; kb < p.kblocks; ++kb) {
+              if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
+                report_status(p.status, DEV_TIMEOUT_EMPTY);
+                *abort_flag = 1;
+                goto producer_done;
+              }
+              if (leader) mbar_arrive_expect_tx(&full[stage], 2 * P_STAGE_BYTES);
+              uint8_t* sa = smem + stage * P_STAGE_BYTES;
+              const uint32_t bar = mapa_shared(&full[stage], 0);
+              tma_load_3d_pair(sa, &tmA, bar, kb * p.kelems, tm * BM, p.pair_a[pi]);
+              tma_load_3d_pair(sa + A_TILE, &tmBh, bar, kb * p.kelems, tn * BN + (int)rank * (BN / 2),
+                               p.pair_b[pi]);
+              if (++stage == PSTAGES) {
+                stage = 0;
+                ph ^= 1;
+              }
+            }
+          }
+        }
+      }
+      if (!aborted(abort_flag)) {
+        // every stage released: no commit from the even CTA is still on its
+        // way to this CTA's barriers
+        for (int i = 0; i < PSTAGES; ++i) {
+          if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
+            report_status(p.status, DEV_TIMEOUT_EMPTY);
+            *abort_flag = 1;
+            break;
+          }
+          if (++stage == PSTAGES) {
+            stage = 0;
+            ph ^= 1;
+          }
+        }
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    // ------------------------------ MMA issuer (even CTA) ------------------------------
+    if (lane == 0 && leader) {
+      const uint32_t idv = tc::idesc(KIND == 0 ? tc::FMT_F16 : tc::FMT_TF32, 2 * BM, BN);
+      int stage = 0;
+      uint32_t ph = 0;
+      int buf = 0;
+      uint32_t acc_ph[2] = {0, 0};
+      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+        for (int g = 0; g < p.ngroups; ++g) {
+          const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
+          const int chunk = p.chunk_kb[g];
+          for (int s0 = 0; s0 < total; s0 += chunk) {
+            if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+              report_status(p.status, DEV_TIMEOUT_TMEM);
+              *abort_flag = 1;
+              goto mma_done;
+            }
+            tc::fence_after();
+            const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+            const int s1 = min(total, s0 + chunk);
+            for (int st = s0; st < s1; ++st) {
+              if (!mbar_wait_bounded(&full[stage], ph)) {
+                report_status(p.status, DEV_TIMEOUT_FULL);
+                *abort_flag = 1;
+                goto mma_done;
+              }
+              tc::fence_after();
+              const uint32_t a_addr = smem_u32(smem + stage * P_STAGE_BYTES);
+              const uint32_t b_addr = a_addr + A_TILE;
+#pragma unroll
+              for (int kk = 0; kk < KSTEPS; ++kk)
+                tc::mma2<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
+                               (st > s0 || kk > 0) ? 1u : 0u);
+              tc::commit2_mc(&empty[stage], (uint16_t)0x3);
+              if (++stage == PSTAGES) {
+                stage = 0;
+                ph ^= 1;
+              }
+            }
+            tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
+          }
+        }
+      }
+    mma_done:
+      if (aborted(abort_flag)) {
+        tc::commit2_mc(drain, (uint16_t)0x1);
+        mbar_wait_bounded(drain, 0);
+      }
+    }
+  } else {
+    // ------------------------------ epilogue (both CTAs) ------------------------------
+    const int q = warp & 3;
+    const int h = (warp - 2) >> 2;
+    const int r_local = q * 32 + lane;
+    const uint32_t tempty_leader[2] = {mapa_shared(&tempty[0], 0), mapa_shared(&tempty[1], 0)};
+    int buf = 0;
+    uint32_t acc_ph[2] = {0, 0};
+    for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+      int tm, tn;
+      coords(t, tm, tn);
+      const int64_t row = (int64_t)tm * BM + r_local;
+      const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
+      typedef typename std::conditional<EPI == EPI_OZAKI, int, float>::type Acc;
+      Acc S[EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+      for (int g = 0; g < p.ngroups; ++g) {
+        const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
+        const int chunk = p.chunk_kb[g];
+        for (int s0 = 0; s0 < total; s0 += chunk) {
+          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+            report_status(p.status, DEV_TIMEOUT_MMA);
+            *abort_flag = 1;
+            goto epi_done;
+          }
+          tc::fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+#pragma unroll
+          for (int pc = 0; pc < EPI_COLS / 16; ++pc) {
+            uint32_t r[16];
+            tc::ld16(taddr + pc * 16, r);
+            tc::ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              if (EPI == EPI_OZAKI) S[pc * 16 + j] += f2i_exact(r[j]);
+              else S[pc * 16 + j] += __uint_as_float(r[j]);
+            }
+          }
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive_cluster(tempty_leader[buf]);
+          acc_ph[buf] ^= 1;
+          buf ^= 1;
+        }
+        if (EPI == EPI_OZAKI) {
+          if (row < p.m) {
+            int* srow = p.sbuf + (size_t)g * p.plane + row;
+#pragma unroll
+            for (int j = 0; j < EPI_COLS; ++j) {
+              const int64_t col = col0 + j;
+              if (col < p.n) srow[col * p.m] = (int)S[j];
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+        }
+      }
+      if (EPI == EPI_F32 && row < p.m) {
+        float* crow = p.c32 + row * p.rsc;
+#pragma unroll
+        for (int j = 0; j < EPI_COLS; ++j) {
+          const int64_t col = col0 + j;
+          if (col < p.n) {
+            float* cp = crow + col * p.csc;
+            const float v = (float)S[j] * p.alpha_f;
+            *cp = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, *cp, v);
+          }
+        }
+      }
+    }
+  epi_done:;
+  }
+
+  __syncwarp();
+  tc::fence_before();
+  __syncthreads();
+  cluster_sync();  // both CTAs are done with each other's barriers and TMEM
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc2(tmem_base, TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 template <int KIND, int EPI>
@@ -367,66 +618,86 @@ inline cudaError_t set_slice_attrs() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              SMEM_BYTES);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(slice_gemm_pair_kernel<KIND, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             P_SMEM_BYTES);
   return e;
 }
 
-// Clusters of two of the multicast kernel that fit on the current device at
-// once (0: none, or multicast switched off by MOMMS_SLICE_MULTICAST=0).
-// Queried once per device.
-template <int KIND, int EPI>
-inline int slice_clusters() {
-  static std::atomic<int> cache[64];
-  static std::atomic<bool> init[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (init[dev].load()) return cache[dev].load();
-  int n = 0;
-  const char* env = getenv("MOMMS_SLICE_MULTICAST");
-  if (!(env && env[0] == '0')) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2);
-    cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (cudaOccupancyMaxActiveClusters(&n, (const void*)slice_gemm_kernel<KIND, EPI, true>, &cfg) != cudaSuccess) {
-      cudaGetLastError();
-      n = 0;
-    }
-  }
-  cache[dev].store(n);
-  init[dev].store(true);
-  return n;
+// Kernel variants: 0 = one CTA per tile, 1 = clusters of two with B
+// multicast, 2 = CTA pairs with cta_group::2 MMA.
+enum { SLICE_SINGLE = 0, SLICE_MULTICAST = 1, SLICE_PAIR = 2 };
+
+inline cudaLaunchConfig_t cluster2_config(const void*, int smem, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2);
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
 }
 
-// Launches the slice kernel: the multicast variant (clusters of two CTAs,
-// tmB_half's box is BN/2 rows) when the device takes clusters and there are
-// at least two m-tiles, otherwise one CTA per SM with tmB_full. Returns
-// whether the multicast variant ran in *mc.
+// The variant to use on the current device and how many clusters of two fit
+// at once; queried once per device. MOMMS_SLICE_VARIANT=0/1/2 restricts the
+// choice to at most that variant (default: the pair kernel).
+template <int KIND, int EPI>
+inline int slice_variant(int* clusters) {
+  static std::atomic<int> cache_v[64], cache_n[64];
+  static std::atomic<bool> init[64];
+  int dev = 0;
+  *clusters = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SLICE_SINGLE;
+  if (!init[dev].load()) {
+    int want = SLICE_PAIR;
+    const char* env = getenv("MOMMS_SLICE_VARIANT");
+    if (env && env[0] >= '0' && env[0] <= '2') want = env[0] - '0';
+    int v = SLICE_SINGLE, n = 0;
+    for (int cand = want; cand >= SLICE_MULTICAST && v == SLICE_SINGLE; --cand) {
+      cudaLaunchAttribute attr[1];
+      const void* fn = cand == SLICE_PAIR ? (const void*)slice_gemm_pair_kernel<KIND, EPI>
+                                          : (const void*)slice_gemm_kernel<KIND, EPI, true>;
+      cudaLaunchConfig_t cfg = cluster2_config(fn, cand == SLICE_PAIR ? P_SMEM_BYTES : SMEM_BYTES, attr);
+      int c = 0;
+      if (cudaOccupancyMaxActiveClusters(&c, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        c = 0;
+      }
+      if (c > 0) {
+        v = cand;
+        n = c;
+      }
+    }
+    cache_v[dev].store(v);
+    cache_n[dev].store(n);
+    init[dev].store(true);
+  }
+  *clusters = cache_n[dev].load();
+  return cache_v[dev].load();
+}
+
+// Launches the slice kernel. The cluster variants need at least two m-tiles
+// (their units are vertical tile pairs) and take tmB_half, whose box is BN/2
+// rows; the single-CTA kernel takes tmB_full. *variant receives the one run.
 template <int KIND, int EPI>
 inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_full, const CUtensorMap& tmB_half,
-                                const Params& p, int sm_count, cudaStream_t s, bool* mc) {
-  const int clusters = p.tiles_m >= 2 ? slice_clusters<KIND, EPI>() : 0;
-  *mc = clusters > 0;
-  if (*mc) {
+                                const Params& p, int sm_count, cudaStream_t s, int* variant) {
+  int clusters = 0;
+  const int v = p.tiles_m >= 2 ? slice_variant<KIND, EPI>(&clusters) : SLICE_SINGLE;
+  *variant = v;
+  if (v != SLICE_SINGLE) {
     const int64_t units = (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
-    cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
-    cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    const void* fn = v == SLICE_PAIR ? (const void*)slice_gemm_pair_kernel<KIND, EPI>
+                                     : (const void*)slice_gemm_kernel<KIND, EPI, true>;
+    cudaLaunchConfig_t cfg = cluster2_config(fn, v == SLICE_PAIR ? P_SMEM_BYTES : SMEM_BYTES, attr);
+    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
+    cfg.stream = s;
+    if (v == SLICE_PAIR) return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, p);
     return cudaLaunchKernelEx(&cfg, slice_gemm_kernel<KIND, EPI, true>, tmA, tmB_half, p);
   }
   const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;

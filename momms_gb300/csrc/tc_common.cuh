@@ -86,6 +86,52 @@ __device__ __forceinline__ void commit_mc(uint64_t* bar, uint16_t mask) {
       : "memory");
 }
 
+// ---- CTA pairs (cta_group::2): one MMA spans the TMEM of both CTAs of a
+// cluster of two. Every tcgen05 instruction of such a kernel uses
+// cta_group::2. The allocation is collective: warp 1 of both CTAs executes it
+// and both receive the same column address.
+__device__ __forceinline__ void tmem_alloc2(uint32_t* smem_dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(smem_dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish2() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc2(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+// Issued by the pair's even CTA: D (M = 256: 128 rows in each CTA's TMEM) +=
+// A (128 rows from each CTA's shared memory) * B^T (N/2 rows from each).
+template <int KIND>
+__device__ __forceinline__ void mma2(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc_v,
+                                     uint32_t accumulate) {
+  if (KIND == 0) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc_v), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc_v), "r"(accumulate)
+        : "memory");
+  }
+}
+// Arrives on the mbarrier at `bar`'s offset in each CTA of `mask` once the
+// pair MMAs issued so far have completed.
+__device__ __forceinline__ void commit2_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
 // ---- TMEM -> registers: 32 lanes x 32 consecutive 32-bit columns ----
 __device__ __forceinline__ void ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
