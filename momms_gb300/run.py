@@ -24,6 +24,8 @@ def main():
     p.add_argument("--target", type=float, default=0.0)
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=1)
+    p.add_argument("--kernels", action="store_true",
+                   help="also report each kernel class's mean time per call (CUDA events per launch)")
     a = p.parse_args()
 
     import torch
@@ -56,9 +58,27 @@ def main():
     ms = e0.elapsed_time(e1) / max(1, a.reps)
     info = mg.CallInfo()
     lib.momms_last_info(ctypes.byref(info))
-    print(json.dumps({"m": a.m, "n": a.n, "k": a.k, "dtype": a.dtype, "prec": a.prec, "ms": ms,
-                      "tflops": 2.0 * a.m * a.n * a.k / (ms * 1e-3) / 1e12, "slices": info.slices,
-                      "pairs": info.pairs, "splits": info.splits}))
+    out = {"m": a.m, "n": a.n, "k": a.k, "dtype": a.dtype, "prec": a.prec, "ms": ms,
+           "tflops": 2.0 * a.m * a.n * a.k / (ms * 1e-3) / 1e12, "slices": info.slices,
+           "pairs": info.pairs, "splits": info.splits, "slice_variant": info.multicast}
+    if a.kernels:
+        # separate timed pass: per-launch events would perturb the whole-call time above
+        lib.momms_timing_enable(1)
+        for _ in range(a.reps):
+            mg.check(lib.momms_gemm(ctypes.byref(d), sp), lib)
+        torch.cuda.synchronize()
+        names = {mg.KERNEL_DGEMM_DMMA: "dgemm_dmma", mg.KERNEL_SGEMM_FFMA: "sgemm_ffma",
+                 mg.KERNEL_SLICE_OZAKI: "slice_ozaki", mg.KERNEL_SLICE_TF32: "slice_tf32",
+                 mg.KERNEL_PREP: "prep", mg.KERNEL_COMBINE: "combine"}
+        per = {}
+        for cls, name in names.items():
+            tot, cnt = ctypes.c_double(), ctypes.c_ulonglong()
+            lib.momms_timing_read(cls, ctypes.byref(tot), ctypes.byref(cnt), 1)
+            if cnt.value:
+                per[name] = tot.value / a.reps
+        lib.momms_timing_enable(0)
+        out["kernel_ms_per_call"] = per
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":
