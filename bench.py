@@ -570,7 +570,9 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": tc_achieved, "peak": tc_peak, "unit": "TFLOP/s",
                      "frac": tc_achieved / tc_peak, "traffic": profile_traffic("slice_gemm_ozaki_8192"),
                      "peak_source": f"bf16 dense cuBLAS burst, {peak_src} (fp16 and bf16 share the tcgen05 rate)",
-                     "kernel": "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>",
+                     "kernel": {2: "momms::sp::slice_gemm_pair_kernel<kind::f16, Ozaki> (cta_group::2 CTA pairs)",
+                                1: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki, multicast>",
+                                0: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>"}.get(info.multicast, "?"),
                      "algorithmic_flops_per_launch": tc_flops_per_launch,
                      "kernel_ms_per_launch": slice_avg,
                      "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps}},

@@ -206,8 +206,8 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   const int tiles_m = (int)ceil_div(g.m, BM), tiles_n = (int)ceil_div(g.n, BN);
   const int64_t tiles = (int64_t)tiles_m * tiles_n;
   const int64_t kblocks = ceil_div(g.k, BK);
-  // Split k only when the output tiles cannot fill the GPU; each split keeps
-  // at least 8 k-blocks.
+  // Split k only when the output tiles cannot fill the GPU (each split keeps
+  // at least two k-blocks; splits_f64).
   int splits = splits_f64(g.m, g.n, g.k, ds->sm_count);
   int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);

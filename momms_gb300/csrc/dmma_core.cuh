@@ -167,6 +167,8 @@ __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2]
         for (int q = 0; q < 2; ++q) store_c(e, row0 + i * 8, col0 + j * 8 + q, acc[i][j][q]);
     return;
   }
+  // Partials exist only for the tile's entries inside C: a small problem's
+  // mostly-empty tile writes and re-reads just its live part.
   const size_t tile_elems = (size_t)BM * BN;
   double* part = tile_partials + (size_t)sp * tile_elems;
 #pragma unroll
@@ -174,7 +176,8 @@ __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2]
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
-      for (int q = 0; q < 2; ++q) part[((i * 4 + j) * 2 + q) * CONSUMERS + ctid] = acc[i][j][q];
+      for (int q = 0; q < 2; ++q)
+        if (row0 + i * 8 < e.m && col0 + j * 8 + q < e.n) part[((i * 4 + j) * 2 + q) * CONSUMERS + ctid] = acc[i][j][q];
   __threadfence();
   consumer_sync();
   if (ctid == 0) {
@@ -190,6 +193,7 @@ __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2]
       for (int j = 0; j < 4; ++j)
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
+          if (row0 + i * 8 >= e.m || col0 + j * 8 + q >= e.n) continue;
           const int r = ((i * 4 + j) * 2 + q) * CONSUMERS + ctid;
           double s = __ldcg(tile_partials + r);
           for (int t = 1; t < splits; ++t) s += __ldcg(tile_partials + (size_t)t * tile_elems + r);
