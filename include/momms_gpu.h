@@ -65,7 +65,7 @@ typedef enum {
   MOMMS_PREC_SPLIT_TF32 = 2  /* f32 only: 3-term split TF32 on tcgen05 */
 } momms_precision;
 
-typedef enum { MOMMS_MEM_AUTO = 0, MOMMS_MEM_HOST = 1, MOMMS_MEM_DEVICE = 2 } momms_memspace;
+typedef enum { MOMMS_MEM_AUTO = 0, MOMMS_MEM_HOST = 1, MOMMS_MEM_DEVICE = 2, MOMMS_MEM_PACKED = 3 } momms_memspace;
 
 /* A strided matrix view: element (i, j) at ptr[i*rs + j*cs]. */
 typedef struct {
@@ -129,6 +129,35 @@ int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float
 int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a,
                         int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
                         int64_t rs_c, int64_t cs_c, void* stream);
+
+/* ---- Packed operands --------------------------------------------------------
+ * An operand used by many calls (a weight matrix, a basis) can be packed once
+ * into the form the kernels read, in device memory: for MOMMS_PREC_OZAKI its
+ * row exponents and `slices` fp16 digit planes, for MOMMS_PREC_SPLIT_TF32 its
+ * two TF32 planes, for MOMMS_PREC_PLAIN a column-major copy with a TMA-ready
+ * leading dimension. A call then names it as an operand with
+ * mem = MOMMS_MEM_PACKED, ptr = the momms_packed handle (rs, cs ignored), and
+ * skips that operand's pre-pass; an emulated call with a packed operand uses
+ * the pack's slice count (both packs must agree) and needs no host round
+ * trip to choose one, so it can be captured in a CUDA graph. Results are
+ * bit-identical to the unpacked call with the same slice count. The
+ * reference's counterpart is its Hierarch matrix type (src/matrix/hierarch.rs:
+ * 18-140), which stores an operand in the blocked layout the algorithm walks
+ * so that no packing happens at run time.
+ *
+ * role: MOMMS_ROLE_A (rows x cols = m x k) or MOMMS_ROLE_B (k x n); the pack
+ * fits only that position and those sizes. src: host or device view (AUTO /
+ * HOST / DEVICE). slices: OZAKI only, 1..16 (0 = 8, the count the FP64-level
+ * target takes for operands without a wide exponent spread). Emulated calls
+ * with k > 65536 cannot use packed operands (their k slabs re-scale per slab).
+ * Synchronous; the pack owns its device memory until momms_packed_destroy. */
+typedef enum { MOMMS_ROLE_A = 0, MOMMS_ROLE_B = 1 } momms_role;
+typedef struct momms_packed_s* momms_packed;
+int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, const momms_operand* src, int slices,
+               void* stream, momms_packed* out);
+int momms_packed_destroy(momms_packed packed);
+/* Device bytes the pack holds. */
+uint64_t momms_packed_bytes(momms_packed packed);
 
 /* ---- Out-of-core (host-resident) GEMMs -----------------------------------
  * A momms_gemm call with host operands whose staged copies plus work space

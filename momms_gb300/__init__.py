@@ -40,6 +40,9 @@ PREC_SPLIT_TF32 = 2
 MEM_AUTO = 0
 MEM_HOST = 1
 MEM_DEVICE = 2
+MEM_PACKED = 3
+ROLE_A = 0
+ROLE_B = 1
 
 
 class Operand(ctypes.Structure):
@@ -175,6 +178,12 @@ def load_library(path=None):
     i64p = ctypes.POINTER(ctypes.c_int64)
     lib.momms_stream_plan.argtypes = [PD, ctypes.c_uint64, i64p, i64p, i64p]
     lib.momms_stream_plan.restype = i32
+    lib.momms_pack.argtypes = [i32, i32, i32, i64, i64, ctypes.POINTER(Operand), i32, vp, ctypes.POINTER(vp)]
+    lib.momms_pack.restype = i32
+    lib.momms_packed_destroy.argtypes = [vp]
+    lib.momms_packed_destroy.restype = i32
+    lib.momms_packed_bytes.argtypes = [vp]
+    lib.momms_packed_bytes.restype = ctypes.c_uint64
     if path is None:
         _lib = lib
     return lib

@@ -198,10 +198,16 @@ int validate(const momms_gemm_desc* d) {
     if (rows[i] == 0 || cols[i] == 0) continue;
     if (i < 2 && (d->m == 0 || d->n == 0)) continue;
     if (!ops[i]->ptr) return fail(MOMMS_ERR_INVALID_ARG, "%c.ptr is null", names[i]);
+    if (ops[i]->mem == MOMMS_MEM_PACKED) {
+      if (i == 2) return fail(MOMMS_ERR_INVALID_ARG, "C cannot be a packed operand");
+      const int rc = check_packed(*d, i, packed_of(*ops[i]));
+      if (rc) return rc;
+      continue;
+    }
     if (ops[i]->rs < 0 || ops[i]->cs < 0) return fail(MOMMS_ERR_INVALID_ARG, "%c has a negative stride", names[i]);
     if ((rows[i] > 1 && ops[i]->rs == 0) || (cols[i] > 1 && ops[i]->cs == 0))
       return fail(MOMMS_ERR_INVALID_ARG, "%c has a zero stride", names[i]);
-    if (ops[i]->mem < MOMMS_MEM_AUTO || ops[i]->mem > MOMMS_MEM_DEVICE)
+    if (ops[i]->mem < MOMMS_MEM_AUTO || ops[i]->mem > MOMMS_MEM_PACKED)
       return fail(MOMMS_ERR_INVALID_ARG, "%c.mem is not a momms_memspace", names[i]);
   }
   // C must not overlap itself: the strides must separate rows and columns.
@@ -265,12 +271,14 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   bool host[3];
   for (int i = 0; i < 3; ++i)
     host[i] = ops[i]->mem == MOMMS_MEM_HOST || (ops[i]->mem == MOMMS_MEM_AUTO && !is_device_ptr(ops[i]->ptr));
+  const bool any_packed = packed_of(d->a) || packed_of(d->b);
   const bool any_host0 = host[0] || host[1] || host[2];
   if (any_host0) {
     // Larger than the staging budget: stream the operands through in blocks
     // (the reference's out-of-core PartM / PartN, src/exper/out_of_core.rs:77-87).
     const uint64_t budget = staging_budget();
     if (incore_bytes(*d, host) > budget) {
+      if (any_packed) return fail(MOMMS_ERR_UNSUPPORTED, "streamed (out-of-core) calls take no packed operands");
       BlockPlan plan;
       rc = plan_blocks(*d, host, budget, &plan);
       if (!rc) rc = gemm_streamed(*d, host, plan, s);
@@ -289,9 +297,13 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   DevMat* dm[3] = {&g.a, &g.b, &g.c};
   const bool any_host = host[0] || host[1] || host[2];
   bool need[3];
+  const DevGemm gv = devgemm_of(*d);  // device views; packed operands resolved
+  g.pk[0] = gv.pk[0];
+  g.pk[1] = gv.pk[1];
+  const DevMat views[3] = {gv.a, gv.b, gv.c};
   for (int i = 0; i < 3; ++i) {
     need[i] = host[i] && (i < 2 || d->beta != 0.0);  // C is read only when beta != 0
-    if (!host[i]) *dm[i] = DevMat{ops[i]->ptr, ops[i]->rs, ops[i]->cs};
+    if (!host[i]) *dm[i] = views[i];
   }
   for (int i = 0; i < 3 && !rc; ++i)
     if (host[i]) {

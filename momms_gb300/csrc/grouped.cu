@@ -278,7 +278,7 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
     if (d.m == 0 || d.n == 0 || d.k == 0) continue;
     const momms_operand* ops[3] = {&d.a, &d.b, &d.c};
     for (int j = 0; j < 3; ++j)
-      if (ops[j]->mem == MOMMS_MEM_HOST || !on_device(ops[j]->ptr))
+      if (!packed_of(*ops[j]) && (ops[j]->mem == MOMMS_MEM_HOST || !on_device(ops[j]->ptr)))
         return fail(MOMMS_ERR_INVALID_ARG, "problem %d: plans take device operands only", i);
   }
   Plan* p = new Plan();
@@ -353,7 +353,8 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
       // tensor maps in each operand's own orientation (repacked copies for
       // strides TMA cannot take, exactly as a single launch does)
       CUtensorMap ma, mb;
-      DevMat a{d.a.ptr, d.a.rs, d.a.cs}, b{d.b.ptr, d.b.rs, d.b.cs};
+      const DevGemm gv = devgemm_of(d);  // packed operands: their column-major copies
+      DevMat a = gv.a, b = gv.b;
       int oa = dmma_orient(a, d.m, d.k, true), ob = dmma_orient(b, d.k, d.n, false);
       if (oa == 2) {
         const int64_t ld = round_up(d.m, 2);
@@ -428,19 +429,22 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
     std::vector<std::pair<double, grouped::SProblem>> items;
     for (int i : slist) {
       const momms_gemm_desc& d = descs[i];
-      if (!((d.a.rs == 1 || d.a.cs == 1) && (d.b.rs == 1 || d.b.cs == 1))) {
+      const DevGemm gv = devgemm_of(d);  // packed operands: their column-major copies
+      const DevMat& va = gv.a;
+      const DevMat& vb = gv.b;
+      if (!((va.rs == 1 || va.cs == 1) && (vb.rs == 1 || vb.cs == 1))) {
         plan_free(p);
         return fail(MOMMS_ERR_INVALID_ARG, "problem %d: grouped f32 operands need unit stride along one index", i);
       }
       grouped::SProblem P;
       memset(&P, 0, sizeof(P));
-      const bool a_xc = (d.a.rs == 1) && !(d.a.cs == 1 && d.m == 1);
-      const bool b_xc = (d.b.cs == 1) && !(d.b.rs == 1 && d.n == 1);
-      const int64_t a_ld = a_xc ? d.a.cs : d.a.rs, b_ld = b_xc ? d.b.rs : d.b.cs;
-      const bool vec = ((reinterpret_cast<uintptr_t>(d.a.ptr) | reinterpret_cast<uintptr_t>(d.b.ptr)) & 15) == 0 &&
+      const bool a_xc = (va.rs == 1) && !(va.cs == 1 && d.m == 1);
+      const bool b_xc = (vb.cs == 1) && !(vb.rs == 1 && d.n == 1);
+      const int64_t a_ld = a_xc ? va.cs : va.rs, b_ld = b_xc ? vb.rs : vb.cs;
+      const bool vec = ((reinterpret_cast<uintptr_t>(va.ptr) | reinterpret_cast<uintptr_t>(vb.ptr)) & 15) == 0 &&
                        a_ld % 4 == 0 && b_ld % 4 == 0;
-      P.o = Operands{static_cast<const float*>(d.a.ptr), d.a.rs, d.a.cs, static_cast<const float*>(d.b.ptr), d.b.rs,
-                     d.b.cs, d.m, d.n, d.k, a_xc, b_xc, vec};
+      P.o = Operands{static_cast<const float*>(va.ptr), va.rs, va.cs, static_cast<const float*>(vb.ptr), vb.rs,
+                     vb.cs, d.m, d.n, d.k, a_xc, b_xc, vec};
       P.e = Epi{d.m, d.n, (float)d.alpha, (float)d.beta, static_cast<float*>(d.c.ptr), d.c.rs, d.c.cs};
       P.tiles_m = (int)ceil_div(d.m, BM);
       P.tiles_n = (int)ceil_div(d.n, BN);
@@ -538,13 +542,7 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
   }
   for (PlanProblem& pp : p->other) {
-    DevGemm g;
-    g.dtype = pp.d.dtype;
-    g.m = pp.d.m; g.n = pp.d.n; g.k = pp.d.k;
-    g.alpha = pp.d.alpha; g.beta = pp.d.beta;
-    g.a = DevMat{pp.d.a.ptr, pp.d.a.rs, pp.d.a.cs};
-    g.b = DevMat{pp.d.b.ptr, pp.d.b.rs, pp.d.b.cs};
-    g.c = DevMat{pp.d.c.ptr, pp.d.c.rs, pp.d.c.cs};
+    const DevGemm g = devgemm_of(pp.d);
     int rc;
     if (pp.d.precision == MOMMS_PREC_OZAKI) {
       int used = 0;

@@ -65,6 +65,29 @@ struct Staging {
   int64_t written = 0;  // columns of C handed to writeback so far
 };
 
+// A packed operand (momms_pack): the device-resident form a kernel reads.
+struct PackedOperand {
+  uint32_t magic = 0;  // kPackMagic while alive
+  int device = -1;
+  int dtype = 0, precision = 0, role = 0;  // role 0 = A (rows m, cols k), 1 = B (rows k, cols n)
+  int64_t rows = 0, cols = 0;
+  void* mem = nullptr;  // the one allocation
+  size_t bytes = 0;
+  // plain: column-major copy, leading dimension ld
+  void* data = nullptr;
+  int64_t ld = 0;
+  // Ozaki / split-TF32: planes [np][R][kp] (R = m for A, n for B; k contiguous)
+  void* planes = nullptr;
+  int np = 0;  // Ozaki: slices; split-TF32: 2
+  int64_t kp = 0;
+  int* exps = nullptr;  // Ozaki: per-row (A) / per-column (B) exponents
+};
+constexpr uint32_t kPackMagic = 0x4D504B31u;
+// The pack behind an operand flagged MOMMS_MEM_PACKED (nullptr otherwise).
+inline const PackedOperand* packed_of(const momms_operand& op) {
+  return op.mem == MOMMS_MEM_PACKED ? static_cast<const PackedOperand*>(op.ptr) : nullptr;
+}
+
 // One GEMM with all operands on the device (or arriving there, see Staging).
 struct DevGemm {
   int dtype;  // momms_dtype
@@ -72,7 +95,14 @@ struct DevGemm {
   double alpha, beta;
   DevMat a, b, c;
   Staging* staging = nullptr;
+  const PackedOperand* pk[2] = {nullptr, nullptr};  // packed A, B (their DevMat is the plain copy, if any)
 };
+
+// DevGemm of a descriptor whose operands are device views or packs.
+DevGemm devgemm_of(const momms_gemm_desc& d);
+bool pack_is_live(const PackedOperand* p);
+// Checks a packed operand against its position (0 = A, 1 = B) in `d`.
+int check_packed(const momms_gemm_desc& d, int which, const PackedOperand* p);
 
 // Make `s` wait until operand `which` (0 = A, 1 = B, 2 = C) is on the device.
 inline cudaError_t wait_operand(const DevGemm& g, int which, cudaStream_t s) {
@@ -147,6 +177,16 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s);
 int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int* slices_used, cudaStream_t s);
 // Accumulation groups (int32 sum planes) of an ns-slice product with this k.
 int ozaki_group_count(int ns, int64_t k);
+// Exponents of the R rows of a view x (element (r, p) at x[r*sr + p*sp],
+// p < K) into exps[R], using maxbits[R] as scratch; and the ns digit planes
+// [ns][R][kp] of the view under those exponents.
+int ozaki_operand_exponents(const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K,
+                            unsigned long long* maxbits, int* exps, cudaStream_t s);
+void ozaki_operand_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, void* planes,
+                          int64_t kp, const int* exps, cudaStream_t s);
+// The two TF32 planes [2][R][kp] of an f32 view.
+void tf32_operand_planes(const float* x, int64_t sr, int64_t sp, int64_t R, int64_t K, float* planes, int64_t kp,
+                         cudaStream_t s);
 
 // Copy an operand into a column-major device scratch matrix with an even
 // leading dimension (used when its strides or alignment do not suit TMA or

@@ -455,22 +455,12 @@ double ozaki_bound(int s, int bits, double q1, double q2) {
 
 // Row exponents of A (first m) and column exponents of B (next n).
 int compute_exponents(const DevGemm& g, unsigned long long* maxbits, int* exps, cudaStream_t s) {
-  const int64_t m = g.m, n = g.n, k = g.k;
-  const double* A = static_cast<const double*>(g.a.ptr);
-  const double* B = static_cast<const double*>(g.b.ptr);
   // A viewed as m x k; B viewed transposed, n x k
-  const bool a_rc = (g.a.rs == 1 && g.a.cs != 1), b_rc = (g.b.cs == 1 && g.b.rs != 1);
-  KernelTimer kt(MOMMS_KERNEL_PREP, s);
-  cudaError_t ce = cudaMemsetAsync(maxbits, 0, (size_t)(m + n) * sizeof(unsigned long long), s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
-  const dim3 blk(32, 8);
-  row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(m, 32)), blk, 0, s>>>(
-      A, g.a.rs, g.a.cs, m, k, a_rc, maxbits);
-  row_absmax_kernel<<<dim3((unsigned)ceil_div(k, 256), (unsigned)ceil_div(n, 32)), blk, 0, s>>>(
-      B, g.b.cs, g.b.rs, n, k, b_rc, maxbits + m);
-  exps_kernel<<<(unsigned)ceil_div(m + n, 256), 256, 0, s>>>(maxbits, m + n, exps);
-  note_launch(3);
-  return MOMMS_OK;
+  int rc = ozaki_operand_exponents(static_cast<const double*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, maxbits, exps, s);
+  if (!rc)
+    rc = ozaki_operand_exponents(static_cast<const double*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, maxbits + g.m,
+                                 exps + g.m, s);
+  return rc;
 }
 
 // Smallest slice count whose sampled worst-case bound meets the target
@@ -511,12 +501,41 @@ int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double tar
 
 }  // namespace
 
+int ozaki_operand_exponents(const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K,
+                            unsigned long long* maxbits, int* exps, cudaStream_t s) {
+  if (R == 0) return MOMMS_OK;
+  const bool r_contig = (sr == 1 && sp != 1);
+  KernelTimer kt(MOMMS_KERNEL_PREP, s);
+  cudaError_t ce = cudaMemsetAsync(maxbits, 0, (size_t)R * sizeof(unsigned long long), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
+  row_absmax_kernel<<<dim3((unsigned)ceil_div(K, 256), (unsigned)ceil_div(R, 32)), dim3(32, 8), 0, s>>>(
+      x, sr, sp, R, K, r_contig, maxbits);
+  exps_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, s>>>(maxbits, R, exps);
+  note_launch(2);
+  ce = cudaGetLastError();
+  return ce == cudaSuccess ? MOMMS_OK : cuda_fail(ce, "Ozaki exponents");
+}
+
+void ozaki_operand_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, void* planes,
+                          int64_t kp, const int* exps, cudaStream_t s) {
+  KernelTimer kt(MOMMS_KERNEL_PREP, s);
+  ozaki_planes(ns, x, sr, sp, R, K, static_cast<__half*>(planes), kp, R * kp, exps, s);
+  note_launch();
+}
+
 int set_attrs_ozaki() {
   cudaError_t e = sp::set_slice_attrs<0, sp::EPI_OZAKI>();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(Ozaki)");
 }
 
 int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
+  // a packed operand fixes the count
+  const PackedOperand* pa = packed_of(d.a);
+  const PackedOperand* pb = packed_of(d.b);
+  if (pa || pb) {
+    *slices = (pa ? pa : pb)->np;
+    return MOMMS_OK;
+  }
   DevGemm g;
   g.dtype = d.dtype;
   g.m = d.m; g.n = d.n; g.k = d.k;
@@ -562,6 +581,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   if (g.k > kMaxK) {
+    if (g.pk[0] || g.pk[1])
+      return fail(MOMMS_ERR_UNSUPPORTED, "packed operands need k <= 65536 (longer k runs in re-scaled slabs)");
     // k slabs of at most 2^16 (the int32 digit sums' range), later slabs
     // accumulating into C with beta = 1 like the reference's PartK
     // (src/composables/part.rs:96-110); each slab meets the target on its own
@@ -586,22 +607,38 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int64_t m = g.m, n = g.n, k = g.k;
   cudaError_t ce;
 
-  // exponents: [m + n] u64 maxima followed by [m + n] int exponents
+  // Packed operands bring their exponents and digit planes, and fix the slice
+  // count (no sampled choice, no host round trip).
+  const PackedOperand* PA = g.pk[0];
+  const PackedOperand* PB = g.pk[1];
+  int ns_fixed = 0;
+  if (PA) ns_fixed = PA->np;
+  if (PB) {
+    if (ns_fixed && PB->np != ns_fixed)
+      return fail(MOMMS_ERR_INVALID_ARG, "packed A has %d slices, packed B %d", ns_fixed, PB->np);
+    ns_fixed = PB->np;
+  }
+  if (ns_fixed && slices > 0 && slices != ns_fixed)
+    return fail(MOMMS_ERR_INVALID_ARG, "desc asks for %d slices, the packed operand holds %d", slices, ns_fixed);
+
+  // exponents of the unpacked operands: [m + n] u64 maxima, [m + n] int exponents
   void* ebuf = nullptr;
   if ((ce = scratch_alloc(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki exponents");
   unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
   int* exps = reinterpret_cast<int*>(maxbits + (m + n));
-  int* rexp = exps;
-  int* cexp = exps + m;
   const double* A = static_cast<const double*>(g.a.ptr);
   const double* B = static_cast<const double*>(g.b.ptr);
   if ((ce = wait_operand(g, 0, s)) != cudaSuccess || (ce = wait_operand(g, 1, s)) != cudaSuccess)
     return cuda_fail(ce, "operand staging");
-  int rc = compute_exponents(g, maxbits, exps, s);
+  int rc = MOMMS_OK;
+  if (!PA) rc = ozaki_operand_exponents(A, g.a.rs, g.a.cs, m, k, maxbits, exps, s);
+  if (!rc && !PB) rc = ozaki_operand_exponents(B, g.b.cs, g.b.rs, n, k, maxbits + m, exps + m, s);
   if (rc) return rc;
+  const int* rexp = PA ? PA->exps : exps;
+  const int* cexp = PB ? PB->exps : exps + m;
 
-  int ns = slices;
+  int ns = ns_fixed ? ns_fixed : slices;
   if (ns <= 0) {
     double bound = 0.0;
     rc = choose_slices(g, rexp, cexp, target, bits, s, &ns, &bound);
@@ -613,16 +650,13 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int64_t kp = round_up(k, 8);  // 16-byte rows of fp16
   const size_t a_plane = (size_t)m * kp, b_plane = (size_t)n * kp;
   __half* planes_buf = nullptr;
-  if ((ce = scratch_alloc(&planes_buf, (size_t)ns * (a_plane + b_plane) * sizeof(__half), s)) != cudaSuccess)
+  const size_t own = (PA ? 0 : (size_t)ns * a_plane) + (PB ? 0 : (size_t)ns * b_plane);
+  if (own && (ce = scratch_alloc(&planes_buf, own * sizeof(__half), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki slice planes");
-  __half* pa = planes_buf;
-  __half* pb = planes_buf + (size_t)ns * a_plane;
-  {
-    KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    ozaki_planes(ns, A, g.a.rs, g.a.cs, m, k, pa, kp, (int64_t)a_plane, rexp, s);
-    ozaki_planes(ns, B, g.b.cs, g.b.rs, n, k, pb, kp, (int64_t)b_plane, cexp, s);
-  }
-  note_launch(2);
+  const __half* pa = PA ? static_cast<const __half*>(PA->planes) : planes_buf;
+  const __half* pb = PB ? static_cast<const __half*>(PB->planes) : planes_buf + (PA ? 0 : (size_t)ns * a_plane);
+  if (!PA) ozaki_operand_planes(ns, A, g.a.rs, g.a.cs, m, k, const_cast<__half*>(pa), kp, rexp, s);
+  if (!PB) ozaki_operand_planes(ns, B, g.b.cs, g.b.rs, n, k, const_cast<__half*>(pb), kp, cexp, s);
 
   if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 per launch");
   CUtensorMap tmA, tmB, tmB_half;
@@ -772,7 +806,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
     if ((rc = columns_done(g, j0, j1, s)) != 0) return rc;
   }
-  cudaFreeAsync(planes_buf, s);
+  if (planes_buf) cudaFreeAsync(planes_buf, s);
   cudaFreeAsync(sbuf, s);
   cudaFreeAsync(ebuf, s);
   return MOMMS_OK;

@@ -277,6 +277,7 @@ int momms_server_submit(momms_server server, const momms_gemm_desc* desc, uint64
   const momms_operand* ops[3] = {&desc->a, &desc->b, &desc->c};
   if (desc->m > 0 && desc->n > 0 && desc->k > 0)
     for (const momms_operand* op : ops) {
+      if (packed_of(*op)) continue;  // packs live in device memory
       cudaPointerAttributes at;
       if (op->mem == MOMMS_MEM_HOST || cudaPointerGetAttributes(&at, op->ptr) != cudaSuccess ||
           !(at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)) {

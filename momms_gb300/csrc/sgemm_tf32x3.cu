@@ -40,30 +40,37 @@ int set_attrs_tf32() {
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(split-TF32)");
 }
 
+void tf32_operand_planes(const float* x, int64_t sr, int64_t sp, int64_t R, int64_t K, float* planes, int64_t kp,
+                         cudaStream_t s) {
+  KernelTimer kt(MOMMS_KERNEL_PREP, s);
+  planes::launch_to_planes(x, sr, sp, R, K, planes, kp, R * kp, Tf32SplitOp{}, s);
+  note_launch();
+}
+
 int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   const int64_t kp = round_up(g.k, 4);  // 16-byte rows for TMA
   const size_t a_plane = (size_t)g.m * kp, b_plane = (size_t)g.n * kp;
+  // packed operands (momms_pack) bring their planes
+  const PackedOperand* PA = g.pk[0];
+  const PackedOperand* PB = g.pk[1];
   void* buf = nullptr;
-  cudaError_t ce = scratch_alloc(&buf, (2 * a_plane + 2 * b_plane) * sizeof(float), s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 planes");
-  float* pa = static_cast<float*>(buf);
-  float* pb = pa + 2 * a_plane;
-  // each operand's split waits only for that operand (timers exclude the waits)
-  if ((ce = wait_operand(g, 0, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
-  {
-    KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    planes::launch_to_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, (int64_t)a_plane,
-                             Tf32SplitOp{}, s);
+  cudaError_t ce = cudaSuccess;
+  const size_t own = (PA ? 0 : 2 * a_plane) + (PB ? 0 : 2 * b_plane);
+  if (own && (ce = scratch_alloc(&buf, own * sizeof(float), s)) != cudaSuccess)
+    return cuda_fail(ce, "split-TF32 planes");
+  float* pa = PA ? static_cast<float*>(PA->planes) : static_cast<float*>(buf);
+  float* pb = PB ? static_cast<float*>(PB->planes) : static_cast<float*>(buf) + (PA ? 0 : 2 * a_plane);
+  // each operand's split waits only for that operand
+  if (!PA) {
+    if ((ce = wait_operand(g, 0, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+    tf32_operand_planes(static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, g.m, g.k, pa, kp, s);
   }
-  if ((ce = wait_operand(g, 1, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
-  {
-    KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    planes::launch_to_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, (int64_t)b_plane,
-                             Tf32SplitOp{}, s);
+  if (!PB) {
+    if ((ce = wait_operand(g, 1, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+    tf32_operand_planes(static_cast<const float*>(g.b.ptr), g.b.cs, g.b.rs, g.n, g.k, pb, kp, s);
   }
-  note_launch(2);
 
   CUtensorMap tmA, tmB, tmB_half;
   {
@@ -118,7 +125,7 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   note_launch();
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 launch");
-  cudaFreeAsync(buf, s);
+  if (buf) cudaFreeAsync(buf, s);
   return MOMMS_OK;
 }
 

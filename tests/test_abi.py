@@ -115,3 +115,18 @@ def test_tune_table_text_roundtrip(lib):
     assert lib.momms_tune_import(b"0 0 1 1 1 99") == mg.ERR_INVALID_ARG
     lib.momms_tune_clear()
     assert lib.momms_tune_export(None, 0, ctypes.byref(need)) == mg.OK and need.value == 1
+
+
+def test_packed_operand_handles_checked_without_a_gpu(lib):
+    """A MOMMS_MEM_PACKED operand must be a live pack: a foreign pointer is
+    refused by validation (looked up, not read); C cannot be packed."""
+    buf = ctypes.create_string_buffer(256)
+    d = gu.make_desc(mg.DTYPE_F64, 8, 8, 8, 1.0, 0.0, (ctypes.addressof(buf), 0, 0), (1, 1, 8), (1, 1, 8))
+    d.a.mem = mg.MEM_PACKED
+    assert lib.momms_gemm_validate(ctypes.byref(d)) == mg.ERR_INVALID_ARG
+    assert b"packed" in lib.momms_last_error()
+    d2 = gu.make_desc(mg.DTYPE_F64, 8, 8, 8, 1.0, 0.0, (1, 1, 8), (1, 1, 8), (ctypes.addressof(buf), 0, 0))
+    d2.c.mem = mg.MEM_PACKED
+    assert lib.momms_gemm_validate(ctypes.byref(d2)) == mg.ERR_INVALID_ARG
+    assert lib.momms_packed_destroy(ctypes.c_void_p(ctypes.addressof(buf))) == mg.ERR_INVALID_ARG
+    assert lib.momms_packed_bytes(ctypes.c_void_p(ctypes.addressof(buf))) == 0
