@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <atomic>
 #include <type_traits>
+#include <vector>
 
 #include "tc_common.cuh"
 
@@ -68,6 +69,7 @@ struct Params {
   int kelems;   // elements per k-block (64 for f16, 32 for tf32: 128 bytes)
   int tiles_m, tiles_n;
   int ngroups;
+  int gchunk;  // groups per work unit: a tile's groups may run as separate units (0 = all)
   int group_begin[MAX_GROUPS + 1];
   int chunk_kb[MAX_GROUPS];
   uint8_t pair_a[MAX_PAIRS], pair_b[MAX_PAIRS];
@@ -123,7 +125,19 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int64_t unit0 = MC ? (int64_t)cluster_id_x() : (int64_t)blockIdx.x;
   const int64_t unit_step = MC ? (int64_t)cluster_count_x() : (int64_t)gridDim.x;
   const int units_m = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
-  const int64_t units = (int64_t)units_m * p.tiles_n;
+  // work unit t: tile (pair) t % tile_units, groups [g_begin(t), g_end(t)) -
+  // group-major, so that units in flight read the same digit planes
+  const int64_t tile_units = (int64_t)units_m * p.tiles_n;
+  const int gchunk = p.gchunk > 0 ? p.gchunk : p.ngroups;
+  const int64_t units = tile_units * ceil_div_dev(p.ngroups, gchunk);
+  auto g_begin = [&](int64_t t) { return (int)(t / tile_units) * gchunk; };
+  auto g_end = [&](int64_t t) { return min(p.ngroups, g_begin(t) + gchunk); };
+  // round r hands units [r*step, (r+1)*step) to the CTAs (clusters), in
+  // reverse order on odd rounds: units are ordered by falling cost (largest
+  // groups first), so this snake order evens out the per-CTA totals
+  auto unit_at = [&](int64_t r) {
+    return r * unit_step + ((r & 1) ? (unit_step - 1 - unit0) : unit0);
+  };
   auto coords = [&](int64_t t, int& tm, int& tn) {
     int um;
     tile_coords<MC ? 8 : 16>(t, units_m, p.tiles_n, um, tn);
@@ -162,10 +176,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       uint32_t armed = 0;  // bit s: stage s has been armed at least once
       uint32_t last_ph = 0;  // bit s: parity of the phase last armed on stage s
-      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+        const int64_t t = unit_at(r);
+        if (t >= units) continue;
         int tm, tn;
-        coords(t, tm, tn);
-        for (int g = 0; g < p.ngroups; ++g) {
+        coords(t % tile_units, tm, tn);
+        for (int g = g_begin(t); g < g_end(t); ++g) {
           for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
             for (int kb = 0; kb < p.kblocks; ++kb) {
               if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
@@ -219,8 +235,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       int buf = 0;
       uint32_t acc_ph[2] = {0, 0};
-      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
-        for (int g = 0; g < p.ngroups; ++g) {
+      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+        const int64_t t = unit_at(r);
+        if (t >= units) continue;
+        for (int g = g_begin(t); g < g_end(t); ++g) {
           const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
           const int chunk = p.chunk_kb[g];
           for (int s0 = 0; s0 < total; s0 += chunk) {
@@ -275,9 +293,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int r_local = q * 32 + lane;
     int buf = 0;
     uint32_t acc_ph[2] = {0, 0};
-    for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+    for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+      const int64_t t = unit_at(r);
+      if (t >= units) continue;
       int tm, tn;
-      coords(t, tm, tn);
+      coords(t % tile_units, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
       // per-thread accumulators of finished chunks: exact int32 digit sums
@@ -287,7 +307,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       Acc S[EPI_COLS];
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
-      for (int g = 0; g < p.ngroups; ++g) {
+      for (int g = g_begin(t); g < g_end(t); ++g) {
         const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
         const int chunk = p.chunk_kb[g];
         for (int s0 = 0; s0 < total; s0 += chunk) {
@@ -393,7 +413,17 @@ __global__ void __launch_bounds__(THREADS, 1)
   const bool leader = (rank == 0);
   const int64_t unit0 = (int64_t)cluster_id_x(), unit_step = (int64_t)cluster_count_x();
   const int units_m = (p.tiles_m + 1) / 2;
-  const int64_t units = (int64_t)units_m * p.tiles_n;
+  const int64_t tile_units = (int64_t)units_m * p.tiles_n;
+  const int gchunk = p.gchunk > 0 ? p.gchunk : p.ngroups;
+  const int64_t units = tile_units * ceil_div_dev(p.ngroups, gchunk);
+  auto g_begin = [&](int64_t t) { return (int)(t / tile_units) * gchunk; };
+  auto g_end = [&](int64_t t) { return min(p.ngroups, g_begin(t) + gchunk); };
+  // round r hands units [r*step, (r+1)*step) to the CTAs (clusters), in
+  // reverse order on odd rounds: units are ordered by falling cost (largest
+  // groups first), so this snake order evens out the per-CTA totals
+  auto unit_at = [&](int64_t r) {
+    return r * unit_step + ((r & 1) ? (unit_step - 1 - unit0) : unit0);
+  };
   auto coords = [&](int64_t t, int& tm, int& tn) {
     int um;
     tile_coords<8>(t, units_m, p.tiles_n, um, tn);
@@ -430,10 +460,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       prefetch_tensormap(&tmBh);
       int stage = 0;
       uint32_t ph = 0;
-      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+        const int64_t t = unit_at(r);
+        if (t >= units) continue;
         int tm, tn;
-        coords(t, tm, tn);
-        for (int g = 0; g < p.ngroups; ++g) {
+        coords(t % tile_units, tm, tn);
+        for (int g = g_begin(t); g < g_end(t); ++g) {
           for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
             for (int kb = 0; kb < p.kblocks; ++kb) {
               if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
@@ -480,8 +512,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       int buf = 0;
       uint32_t acc_ph[2] = {0, 0};
-      for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
-        for (int g = 0; g < p.ngroups; ++g) {
+      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+        const int64_t t = unit_at(r);
+        if (t >= units) continue;
+        for (int g = g_begin(t); g < g_end(t); ++g) {
           const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
           const int chunk = p.chunk_kb[g];
           for (int s0 = 0; s0 < total; s0 += chunk) {
@@ -532,16 +566,18 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t tempty_leader[2] = {mapa_shared(&tempty[0], 0), mapa_shared(&tempty[1], 0)};
     int buf = 0;
     uint32_t acc_ph[2] = {0, 0};
-    for (int64_t t = unit0; t < units && !aborted(abort_flag); t += unit_step) {
+    for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
+      const int64_t t = unit_at(r);
+      if (t >= units) continue;
       int tm, tn;
-      coords(t, tm, tn);
+      coords(t % tile_units, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
       typedef typename std::conditional<EPI == EPI_OZAKI, int, float>::type Acc;
       Acc S[EPI_COLS];
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
-      for (int g = 0; g < p.ngroups; ++g) {
+      for (int g = g_begin(t); g < g_end(t); ++g) {
         const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
         const int chunk = p.chunk_kb[g];
         for (int s0 = 0; s0 < total; s0 += chunk) {
@@ -689,20 +725,50 @@ inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_f
   int clusters = 0;
   const int v = p.tiles_m >= 2 ? slice_variant<KIND, EPI>(&clusters) : SLICE_SINGLE;
   *variant = v;
+  const int64_t tile_units = v != SLICE_SINGLE ? (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n
+                                               : (int64_t)p.tiles_m * p.tiles_n;
+  const int64_t slots = v != SLICE_SINGLE ? clusters : sm_count;
+  Params q = p;
+  q.gchunk = p.ngroups;
+  // Few tiles: a tile's accumulation groups (each writes its own int32 plane)
+  // can run as separate work units. Pick the split whose schedule of units
+  // (group-major, handed out in the kernel's snake order; cost = k-blocks of
+  // the unit's pairs plus 8 for its pipeline fill) finishes first.
+  if (EPI == EPI_OZAKI && tile_units < 4 * slots && p.ngroups > 1) {
+    double best = -1.0;
+    std::vector<double> load((size_t)slots);
+    for (int gc = p.ngroups; gc >= 1; gc = gc == 1 ? 0 : (gc + 1) / 2) {
+      std::fill(load.begin(), load.end(), 0.0);
+      const int chunks = (p.ngroups + gc - 1) / gc;
+      int64_t u = 0;
+      for (int c = 0; c < chunks; ++c) {
+        const int g0 = c * gc, g1 = std::min(p.ngroups, g0 + gc);
+        const double cost = 8.0 + (double)(p.group_begin[g1] - p.group_begin[g0]) * (double)p.kblocks;
+        for (int64_t tu = 0; tu < tile_units; ++tu, ++u) {
+          const int64_t r = u / slots, i = u % slots;
+          load[(size_t)((r & 1) ? slots - 1 - i : i)] += cost;  // the kernel's snake order
+        }
+      }
+      const double makespan = *std::max_element(load.begin(), load.end());
+      if (best < 0.0 || makespan < best * 0.97) {  // a finer split must gain 3 %
+        best = makespan;
+        q.gchunk = gc;
+      }
+    }
+  }
+  const int64_t units = tile_units * ((p.ngroups + q.gchunk - 1) / q.gchunk);
   if (v != SLICE_SINGLE) {
-    const int64_t units = (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n;
     cudaLaunchAttribute attr[1];
     const void* fn = v == SLICE_PAIR ? (const void*)slice_gemm_pair_kernel<KIND, EPI>
                                      : (const void*)slice_gemm_kernel<KIND, EPI, true>;
     cudaLaunchConfig_t cfg = cluster2_config(fn, v == SLICE_PAIR ? P_SMEM_BYTES : SMEM_BYTES, attr);
     cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
     cfg.stream = s;
-    if (v == SLICE_PAIR) return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, p);
-    return cudaLaunchKernelEx(&cfg, slice_gemm_kernel<KIND, EPI, true>, tmA, tmB_half, p);
+    if (v == SLICE_PAIR) return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, q);
+    return cudaLaunchKernelEx(&cfg, slice_gemm_kernel<KIND, EPI, true>, tmA, tmB_half, q);
   }
-  const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
-  const int grid = (int)std::min<int64_t>(tiles, sm_count);
-  slice_gemm_kernel<KIND, EPI, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, p);
+  const int grid = (int)std::min<int64_t>(units, sm_count);
+  slice_gemm_kernel<KIND, EPI, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, q);
   return cudaGetLastError();
 }
 
