@@ -591,7 +591,13 @@ def run_ours(args):
 
     # ---- rooflines ----
     peaks, peak_src = _measured_peaks()
-    tc_flops_per_launch = info.pairs * flops  # fp16 MMA work of the slice kernel
+    # fp16 MMA work of one slice-kernel launch: a call runs one launch per
+    # column chunk of C, each over its share of the columns
+    slice_per_step = max(1, round(slice_n / max(1, args.steps)))
+    tc_flops_per_launch = info.pairs * flops / slice_per_step
+    slice_traffic = profile_traffic("slice_gemm_ozaki_8192")  # one unchunked 8192^3 launch
+    if slice_traffic is not None:
+        slice_traffic /= slice_per_step
     slice_avg = slice_ms / max(1, slice_n)
     tc_achieved = tc_flops_per_launch / (slice_avg * 1e-3) / 1e12
     tc_peak = float(peaks["bf16_tflops"])
@@ -625,13 +631,13 @@ def run_ours(args):
                                "kernel": "momms::dmma::dgemm_kernel"}},
         "speedup_emulated_vs_plain": value / (flops / (statistics.mean(plain_ms) * 1e-3) / 1e12),
         "roofline": {"bound": "tensor", "achieved": tc_achieved, "peak": tc_peak, "unit": "TFLOP/s",
-                     "frac": tc_achieved / tc_peak, "traffic": profile_traffic("slice_gemm_ozaki_8192"),
+                     "frac": tc_achieved / tc_peak, "traffic": slice_traffic,
                      "peak_source": f"bf16 dense cuBLAS burst, {peak_src} (fp16 and bf16 share the tcgen05 rate)",
                      "kernel": {2: "momms::sp::slice_gemm_pair_kernel<kind::f16, Ozaki> (cta_group::2 CTA pairs)",
                                 1: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki, multicast>",
                                 0: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>"}.get(info.multicast, "?"),
                      "algorithmic_flops_per_launch": tc_flops_per_launch,
-                     "kernel_ms_per_launch": slice_avg,
+                     "kernel_ms_per_launch": slice_avg, "launches_per_step": slice_per_step,
                      "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps}},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "api": "momms_gemm, MOMMS_PREC_OZAKI, MOMMS_MEM_HOST pinned operands"},

@@ -79,14 +79,16 @@ DeviceState* device_state() {
     }
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    cudaStream_t cs = nullptr, cs2 = nullptr;
+    cudaStream_t cs = nullptr, cs2 = nullptr, aux = nullptr;
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking)) != cudaSuccess) {
-      cuda_fail(e, "copy stream");
+        (e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) != cudaSuccess) {
+      cuda_fail(e, "library stream");
       return nullptr;
     }
     d.copy_stream = cs;
     d.copy_stream2 = cs2;
+    d.aux = aux;
     d.pool = pool;
     d.sm_count = sms;
     d.status = st;
@@ -215,27 +217,44 @@ int validate(const momms_gemm_desc* d) {
   return MOMMS_OK;
 }
 
+// Per-call staging state: the hooks the launchers see, the copy streams
+// (host->device on `copy`, device->host on `back`) and the call's events
+// (ev 0-2: A, B, C copied in; 3: buffers allocated; 4, 5: copy streams done).
 struct StagedCall {
   Staging hooks;
-  cudaStream_t copy = nullptr;
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t cols_ev = nullptr;  // C columns final on the compute stream (re-recorded per range)
-  const momms_operand* c_op = nullptr;
-  const Staged* c_st = nullptr;
+  cudaStream_t copy = nullptr, back = nullptr;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> col_ev;  // column copies (deferred operands) and write-back ranges
+  const momms_operand* ops[3] = {nullptr, nullptr, nullptr};
+  const Staged* st = nullptr;
   size_t es = 0;
   ~StagedCall() {
-    if (cols_ev) cudaEventDestroy(cols_ev);
+    for (cudaEvent_t e : col_ev) cudaEventDestroy(e);
+  }
+  cudaError_t new_event(cudaEvent_t* e) {
+    cudaError_t r = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+    if (r == cudaSuccess) col_ev.push_back(*e);
+    return r;
   }
 };
 
 int writeback_cols(Staging* h, int64_t j0, int64_t j1, cudaStream_t s) {
   StagedCall* sc = static_cast<StagedCall*>(h->ctx);
-  cudaError_t e = cudaSuccess;
-  if (!sc->cols_ev) e = cudaEventCreateWithFlags(&sc->cols_ev, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventRecord(sc->cols_ev, s);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(sc->copy, sc->cols_ev, 0);
+  cudaEvent_t ev = nullptr;
+  cudaError_t e = sc->new_event(&ev);
+  if (e == cudaSuccess) e = cudaEventRecord(ev, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(sc->back, ev, 0);
   if (e != cudaSuccess) return cuda_fail(e, "C copy-back");
-  return stage_out_cols(*sc->c_op, sc->es, *sc->c_st, j0, j1, sc->copy);
+  return stage_out_cols(*sc->ops[2], sc->es, sc->st[2], j0, j1, sc->back);
+}
+
+int copy_cols_in(Staging* h, int which, int64_t j0, int64_t j1, cudaEvent_t* done) {
+  StagedCall* sc = static_cast<StagedCall*>(h->ctx);
+  int rc = stage_in_cols(*sc->ops[which], sc->es, sc->st[which], j0, j1, sc->copy);
+  if (rc || !done) return rc;
+  cudaError_t e = sc->new_event(done);
+  if (e == cudaSuccess) e = cudaEventRecord(*done, sc->copy);
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "staging events");
 }
 
 int dispatch(const DevGemm& g, const momms_gemm_desc* d, cudaStream_t s) {
@@ -323,26 +342,33 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   const bool overlap = any_host && cap == cudaStreamCaptureStatusNone && ds && ds->copy_stream;
   StagedCall sc;
   sc.copy = overlap ? ds->copy_stream : s;
-  sc.c_op = ops[2];
-  sc.c_st = &st[2];
+  sc.back = overlap ? ds->copy_stream2 : s;
+  for (int i = 0; i < 3; ++i) sc.ops[i] = ops[i];
+  sc.st = st;
   sc.es = es;
   if (!rc && overlap) {
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sc.ev[i], cudaEventDisableTiming);
-    // the copy stream starts after the staging buffers exist (allocated on s)
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sc.ev[i], cudaEventDisableTiming);
+    // the copy streams start after the staging buffers exist (allocated on s)
     if (e == cudaSuccess) e = cudaEventRecord(sc.ev[3], s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(sc.copy, sc.ev[3], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(sc.back, sc.ev[3], 0);
     if (e != cudaSuccess) rc = cuda_fail(e, "staging events");
+    sc.hooks.ctx = &sc;
+    sc.hooks.copy_cols = copy_cols_in;
     for (int i = 0; i < 3 && !rc; ++i)
       if (need[i]) {
+        // The emulated path reads B and C by column ranges and enqueues
+        // their copies itself, in the order it needs them.
+        if (i > 0 && d->precision == MOMMS_PREC_OZAKI && plain_pitch(*ops[i], st[i])) {
+          sc.hooks.deferred[i] = true;
+          continue;
+        }
         rc = stage_copy_in(*ops[i], es, st[i], sc.copy);
         if (!rc && (e = cudaEventRecord(sc.ev[i], sc.copy)) != cudaSuccess) rc = cuda_fail(e, "staging events");
         if (!rc) sc.hooks.ready[i] = sc.ev[i];
       }
-    if (host[2] && plain_pitch(*ops[2], st[2])) {
-      sc.hooks.writeback = writeback_cols;
-      sc.hooks.ctx = &sc;
-    }
+    if (host[2] && plain_pitch(*ops[2], st[2])) sc.hooks.writeback = writeback_cols;
     g.staging = &sc.hooks;
   } else {
     for (int i = 0; i < 3 && !rc; ++i)
@@ -354,10 +380,12 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
     if (sc.hooks.writeback) rc = columns_done(g, sc.hooks.written, g.n, s);  // what the path left
     else rc = stage_out(*ops[2], es, st[2], s);
   }
-  if (overlap && sc.ev[4]) {
-    // s (and so the frees below) waits for everything on the copy stream
+  if (overlap && sc.ev[5]) {
+    // s (and so the frees below) waits for everything on the copy streams
     cudaError_t e = cudaEventRecord(sc.ev[4], sc.copy);
+    if (e == cudaSuccess) e = cudaEventRecord(sc.ev[5], sc.back);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, sc.ev[4], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, sc.ev[5], 0);
     if (!rc && e != cudaSuccess) rc = cuda_fail(e, "staging events");
   }
   for (int i = 0; i < 3; ++i)
@@ -366,7 +394,7 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (!rc && e != cudaSuccess) rc = cuda_fail(e, "stream synchronize");
   }
-  for (int i = 0; i < 5; ++i)
+  for (int i = 0; i < 6; ++i)
     if (sc.ev[i]) cudaEventDestroy(sc.ev[i]);
   if (!rc) g_last_info = g_info;
   return rc;

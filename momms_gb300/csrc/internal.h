@@ -17,7 +17,8 @@ struct DeviceState {
   unsigned* status = nullptr;  // device status word (see DEV_* bits)
   cudaMemPool_t pool = nullptr;  // the library's stream-ordered scratch pool
   cudaStream_t copy_stream = nullptr;   // host->device staging copies of momms_gemm calls
-  cudaStream_t copy_stream2 = nullptr;  // device->host copies of streamed (out-of-core) calls
+  cudaStream_t copy_stream2 = nullptr;  // device->host copies (streamed calls, C write-back)
+  cudaStream_t aux = nullptr;           // second compute stream of column-chunked emulated calls
 };
 
 // Stream-ordered scratch allocation (free with cudaFreeAsync) from the
@@ -63,6 +64,11 @@ struct Staging {
   int (*writeback)(Staging* st, int64_t j0, int64_t j1, cudaStream_t s) = nullptr;
   void* ctx = nullptr;
   int64_t written = 0;  // columns of C handed to writeback so far
+  // Deferred operands (B, C): not copied in yet; the launcher enqueues their
+  // column ranges with copy_cols in the order it will read them. `done`
+  // (may be null) receives an event marking the copy, owned by the call.
+  bool deferred[3] = {false, false, false};
+  int (*copy_cols)(Staging* st, int which, int64_t j0, int64_t j1, cudaEvent_t* done) = nullptr;
 };
 
 // A packed operand (momms_pack): the device-resident form a kernel reads.
@@ -114,6 +120,13 @@ inline cudaError_t wait_operands(const DevGemm& g, cudaStream_t s) {
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = wait_operand(g, i, s);
   return e;
 }
+// Enqueue the copy of a deferred operand's columns [j0, j1) (nothing for an
+// operand already on the device; *done is then null).
+inline int copy_columns(const DevGemm& g, int which, int64_t j0, int64_t j1, cudaEvent_t* done) {
+  if (done) *done = nullptr;
+  if (!g.staging || !g.staging->deferred[which] || j1 <= j0) return 0;
+  return g.staging->copy_cols(g.staging, which, j0, j1, done);
+}
 // C's columns [j0, j1) are final in stream order on `s`.
 inline int columns_done(const DevGemm& g, int64_t j0, int64_t j1, cudaStream_t s) {
   if (!g.staging || !g.staging->writeback || j1 <= j0) return 0;
@@ -138,6 +151,8 @@ int stage_alloc(const momms_operand& op, int64_t rows, int64_t cols, size_t es, 
 // The view's unit stride runs along the device copy's inner index with room
 // for it: one 2-D memcpy each way (otherwise the host gathers / scatters).
 bool plain_pitch(const momms_operand& op, const Staged& st);
+// Host -> device copy of columns [j0, j1) of a plain-pitch view.
+int stage_in_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s);
 int stage_copy_in(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s);
 int stage_out_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s);
 int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t s);

@@ -25,7 +25,9 @@
 // (digit truncation of A and B, then the largest dropped diagonal).
 #include <cuda_fp16.h>
 #include <math.h>
+#include <stdlib.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "internal.h"
@@ -91,16 +93,18 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restric
 
 // Exponent e with max |x| < 2^e (the frexp exponent of the maximum); 0 for an
 // all-zero row; INT32_MAX for a row holding a NaN or an infinity.
+// Exponent e of a row whose largest |v| has bit pattern b: |v| < 2^e.
+__device__ __forceinline__ int exponent_of_max(unsigned long long b) {
+  if (b >= 0x7ff0000000000000ull) return INT32_MAX;
+  if (b == 0) return 0;
+  if ((b >> 52) != 0) return (int)(b >> 52) - 1022;  // [2^(be-1023), 2^(be-1022))
+  return (63 - __clzll((long long)b)) - 1073;         // subnormal
+}
+
 __global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int64_t count, int* __restrict__ exps) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  const unsigned long long b = maxbits[i];
-  int e;
-  if (b >= 0x7ff0000000000000ull) e = INT32_MAX;
-  else if (b == 0) e = 0;
-  else if ((b >> 52) != 0) e = (int)(b >> 52) - 1022;  // [2^(be-1023), 2^(be-1022))
-  else e = (63 - __clzll((long long)b)) - 1073;         // subnormal
-  exps[i] = e;
+  exps[i] = exponent_of_max(maxbits[i]);
 }
 
 // Signed digits of v * 2^-e at kDigitBits bits each, nearest rounding at the
@@ -212,7 +216,8 @@ void ozaki_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, in
 constexpr int kSampleRowBlocks = 8, kSampleCols = 8, kSamples = kSampleRowBlocks * kSampleCols;
 constexpr int kSampleSlot = 2 * 32 + 1;  // sab[32], sa[32], sb
 
-__device__ __forceinline__ void sample_position(int x, int y, int64_t m, int64_t n, int64_t* i0, int64_t* j) {
+__host__ __device__ __forceinline__ void sample_position(int x, int y, int64_t m, int64_t n, int64_t* i0,
+                                                         int64_t* j) {
   uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(x * 131 + y * 7 + 1);
   h ^= h >> 31;
   h *= 0xBF58476D1CE4E5B9ull;
@@ -270,6 +275,27 @@ __global__ void __launch_bounds__(256) sample_partial_kernel(const double* __res
       for (int w = 0; w < 8; ++w) t += s_b[w];
       slot[64] = t;
     }
+  }
+}
+
+// Column exponents of B at the sampled columns only (the same values the
+// per-column scan gives), so that the slice count can be chosen before the
+// rest of B is on the device. Samples sharing a column write the same value.
+__global__ void __launch_bounds__(256) sample_col_exps_kernel(const double* __restrict__ b, int64_t rsb, int64_t csb,
+                                                              int64_t m, int64_t n, int64_t k,
+                                                              int* __restrict__ cexp) {
+  __shared__ unsigned long long red[8];
+  int64_t i0, j;
+  sample_position(blockIdx.x % kSampleRowBlocks, blockIdx.x / kSampleRowBlocks, m, n, &i0, &j);
+  unsigned long long mx = 0;
+  for (int64_t pp = threadIdx.x; pp < k; pp += 256) mx = max(mx, abs_bits(b[pp * rsb + j * csb]));
+#pragma unroll
+  for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) mx = max(mx, red[w]);
+    cexp[j] = exponent_of_max(mx);
   }
 }
 
@@ -577,6 +603,29 @@ int ozaki_group_count(int ns, int64_t k) {
   return ng;
 }
 
+namespace {
+constexpr int kMaxChunks = 8;
+
+// Column chunks of one emulated call: n cut at multiples of the tile width.
+// Calls whose B / C arrive from host memory take 4 chunks of at least 1024
+// columns (4096^3: e2e 5.40 -> 4.60 ms, 8192^3: 31.2 -> 28.3 ms; 6 or 8
+// chunks were no better); device-resident calls of at least 2^36 flops take
+// chunks of at least 2048 columns, which fill the products' tail with the
+// next chunk's preparation (4096^3: 3.53 -> 3.48 ms).
+// MOMMS_OZAKI_CHUNKS=1..8 fixes the count for A/B measurements; the results
+// are the same for every count (each entry's sums do not depend on it).
+int column_chunks(int64_t m, int64_t n, int64_t k, bool deferred) {
+  const char* env = getenv("MOMMS_OZAKI_CHUNKS");
+  if (env && *env) {
+    const int v = atoi(env);
+    if (v >= 1 && v <= kMaxChunks) return (int)std::min<int64_t>(v, ceil_div(n, sp::BN));
+  }
+  if (deferred) return (int)std::max<int64_t>(1, std::min<int64_t>(4, n / 1024));
+  if ((double)m * (double)n * (double)k < 6.0e10) return 1;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(4, n / 2048));
+}
+}  // namespace
+
 int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
@@ -587,6 +636,15 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     // accumulating into C with beta = 1 like the reference's PartK
     // (src/composables/part.rs:96-110); each slab meets the target on its own
     const int64_t nslab = ceil_div(g.k, kMaxK), kb = round_up(ceil_div(g.k, nslab), 64);
+    // deferred B / C arrive whole before the first slab
+    for (int w = 1; w <= 2 && g.staging; ++w)
+      if (g.staging->deferred[w]) {
+        cudaEvent_t ev = nullptr;
+        const int rc = copy_columns(g, w, 0, g.n, &ev);
+        if (rc) return rc;
+        g.staging->deferred[w] = false;
+        g.staging->ready[w] = ev;
+      }
     for (int64_t p0 = 0; p0 < g.k; p0 += kb) {
       DevGemm gs = g;
       gs.k = std::min(kb, g.k - p0);
@@ -621,6 +679,49 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   if (ns_fixed && slices > 0 && slices != ns_fixed)
     return fail(MOMMS_ERR_INVALID_ARG, "desc asks for %d slices, the packed operand holds %d", slices, ns_fixed);
 
+  // Column chunks (column_chunks): chunk c runs on s (even c) or the
+  // device's second compute stream (odd c), so that chunk c+1's B
+  // preparation and chunk c's recombination fill the tail of chunk c's slice
+  // products, and deferred B / C columns arrive a chunk ahead of their use.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
+  Staging* stg = g.staging;
+  const bool defer_b = stg && stg->deferred[1], defer_c = stg && stg->deferred[2];
+  const int nch = (cap == cudaStreamCaptureStatusNone && ds->aux) ? column_chunks(m, n, k, defer_b || defer_c) : 1;
+  int64_t cut[kMaxChunks + 1];
+  for (int c = 0; c < nch; ++c) cut[c] = std::min<int64_t>(n, round_up(n * c / nch, sp::BN));
+  cut[nch] = n;
+  const bool choose = ns_fixed == 0 && slices <= 0;
+
+  // Deferred copies in the order they are read: B's sampled columns (the
+  // slice-count choice needs only those), then B's chunks, each C chunk one
+  // behind its B chunk.
+  cudaEvent_t ev_sample = nullptr, ev_b[kMaxChunks] = {}, ev_c[kMaxChunks] = {};
+  int rc = MOMMS_OK;
+  if (defer_b && choose) {
+    int64_t js[kSamples];
+    for (int q = 0; q < kSamples; ++q) {
+      int64_t i0;
+      sample_position(q % kSampleRowBlocks, q / kSampleRowBlocks, m, n, &i0, &js[q]);
+    }
+    std::sort(js, js + kSamples);
+    for (int q = 0; q < kSamples && !rc;) {
+      int r = q + 1;
+      while (r < kSamples && js[r] <= js[r - 1] + 1) ++r;  // a run of adjacent or repeated columns
+      rc = copy_columns(g, 1, js[q], js[r - 1] + 1, r == kSamples ? &ev_sample : nullptr);
+      q = r;
+    }
+  }
+  for (int c = 0; c < nch && !rc; ++c) {
+    if (defer_b) rc = copy_columns(g, 1, cut[c], cut[c + 1], &ev_b[c]);
+    if (!rc && defer_c && c > 0) rc = copy_columns(g, 2, cut[c - 1], cut[c], &ev_c[c - 1]);
+  }
+  if (!rc && defer_c) rc = copy_columns(g, 2, cut[nch - 1], cut[nch], &ev_c[nch - 1]);
+  if (rc) return rc;
+
   // exponents of the unpacked operands: [m + n] u64 maxima, [m + n] int exponents
   void* ebuf = nullptr;
   if ((ce = scratch_alloc(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
@@ -629,19 +730,25 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   int* exps = reinterpret_cast<int*>(maxbits + (m + n));
   const double* A = static_cast<const double*>(g.a.ptr);
   const double* B = static_cast<const double*>(g.b.ptr);
-  if ((ce = wait_operand(g, 0, s)) != cudaSuccess || (ce = wait_operand(g, 1, s)) != cudaSuccess)
-    return cuda_fail(ce, "operand staging");
-  int rc = MOMMS_OK;
+  if ((ce = wait_operand(g, 0, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   if (!PA) rc = ozaki_operand_exponents(A, g.a.rs, g.a.cs, m, k, maxbits, exps, s);
-  if (!rc && !PB) rc = ozaki_operand_exponents(B, g.b.cs, g.b.rs, n, k, maxbits + m, exps + m, s);
   if (rc) return rc;
   const int* rexp = PA ? PA->exps : exps;
-  const int* cexp = PB ? PB->exps : exps + m;
+  int* cexp_w = exps + m;  // B's column exponents, written per chunk
+  const int* cexp = PB ? PB->exps : cexp_w;
 
   int ns = ns_fixed ? ns_fixed : slices;
   if (ns <= 0) {
+    // B at the sampled columns, and their exponents
+    ce = defer_b ? cudaStreamWaitEvent(s, ev_sample, 0) : wait_operand(g, 1, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "operand staging");
+    {
+      KernelTimer kt(MOMMS_KERNEL_PREP, s);
+      sample_col_exps_kernel<<<kSamples, 256, 0, s>>>(B, g.b.rs, g.b.cs, m, n, k, cexp_w);
+    }
+    note_launch();
     double bound = 0.0;
-    rc = choose_slices(g, rexp, cexp, target, bits, s, &ns, &bound);
+    rc = choose_slices(g, rexp, cexp_w, target, bits, s, &ns, &bound);
     if (rc) return rc;
     call_info().bound_rel_err = bound;
   }
@@ -656,35 +763,23 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const __half* pa = PA ? static_cast<const __half*>(PA->planes) : planes_buf;
   const __half* pb = PB ? static_cast<const __half*>(PB->planes) : planes_buf + (PA ? 0 : (size_t)ns * a_plane);
   if (!PA) ozaki_operand_planes(ns, A, g.a.rs, g.a.cs, m, k, const_cast<__half*>(pa), kp, rexp, s);
-  if (!PB) ozaki_operand_planes(ns, B, g.b.cs, g.b.rs, n, k, const_cast<__half*>(pb), kp, cexp, s);
 
   if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 per launch");
-  CUtensorMap tmA, tmB, tmB_half;
+  CUtensorMap tmA;
   {
     uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)ns};
     uint64_t strides[2] = {(uint64_t)kp * 2, (uint64_t)a_plane * 2};
     uint32_t box[3] = {64, (uint32_t)sp::BM, 1};  // 128-byte k-blocks
-    int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
-    if (rc) return rc;
-    uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)ns};
-    uint64_t stridesb[2] = {(uint64_t)kp * 2, (uint64_t)b_plane * 2};
-    uint32_t boxb[3] = {64, (uint32_t)sp::BN, 1};
-    rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
-    if (rc) return rc;
-    uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
-    rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb, dimsb, stridesb, boxh,
-                      CU_TENSOR_MAP_SWIZZLE_128B);
+    rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pa, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
   }
 
   sp::Params p;
   memset(&p, 0, sizeof(p));
   p.m = m;
-  p.n = n;
   p.kelems = 64;
   p.kblocks = (int)ceil_div(k, 64);
   p.tiles_m = (int)ceil_div(m, sp::BM);
-  p.tiles_n = (int)ceil_div(n, sp::BN);
   CombineParams cp;
   memset(&cp, 0, sizeof(cp));
   uint8_t dgrp[sp::MAX_GROUPS];  // level (d - 2) of each group
@@ -732,18 +827,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const size_t plane = (size_t)m * n;
   if ((ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki group sums");
-  p.sbuf = sbuf;
   p.plane = (int64_t)plane;
   p.status = ds->status;
-
-  {
-    KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, s);
-    int variant = 0;
-    ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, s, &variant);
-    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki slice launch");
-    call_info().multicast = variant;
-  }
-  note_launch();
 
   cp.sbuf = sbuf;
   cp.plane = (int64_t)plane;
@@ -787,29 +872,100 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.c = static_cast<double*>(g.c.ptr);
   cp.rsc = g.c.rs;
   cp.csc = g.c.cs;
-  if ((ce = wait_operand(g, 2, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
-  // With C staged from host memory the recombination runs in column ranges,
-  // each copied back while the next is computed.
-  const int64_t nchunks = (g.staging && g.staging->writeback) ? std::min<int64_t>(4, n) : 1;
-  for (int64_t ch = 0; ch < nchunks; ++ch) {
-    const int64_t j0 = n * ch / nchunks, j1 = n * (ch + 1) / nchunks;
-    cp.j0 = j0;
-    cp.j1 = j1;
-    const int64_t bx = ceil_div(m, 512);
-    const int64_t by = std::min<int64_t>({j1 - j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
+
+  // the second stream starts after everything above (scratch, A, the choice)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  if (nch > 1) {
+    ce = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev_fork, s);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ds->aux, ev_fork, 0);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+  }
+  for (int c = 0; c < nch && !rc; ++c) {
+    const int64_t j0 = cut[c], j1 = cut[c + 1], w = j1 - j0;
+    if (w <= 0) continue;
+    cudaStream_t X = (c & 1) ? ds->aux : s;
+    // B's columns j0..j1: exponents and digit planes
+    ce = defer_b ? cudaStreamWaitEvent(X, ev_b[c], 0) : wait_operand(g, 1, X);
+    if (ce != cudaSuccess) {
+      rc = cuda_fail(ce, "operand staging");
+      break;
+    }
+    const double* Bc = B + j0 * g.b.cs;
+    if (!PB) {
+      rc = ozaki_operand_exponents(Bc, g.b.cs, g.b.rs, w, k, maxbits + m + j0, cexp_w + j0, X);
+      if (rc) break;
+      KernelTimer kt(MOMMS_KERNEL_PREP, X);
+      ozaki_planes(ns, Bc, g.b.cs, g.b.rs, w, k, const_cast<__half*>(pb) + j0 * kp, kp, (int64_t)b_plane,
+                   cexp_w + j0, X);
+      note_launch();
+    }
+    CUtensorMap tmB, tmB_half;
     {
-      KernelTimer kt(MOMMS_KERNEL_COMBINE, s);
-      combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, s>>>(cp);
+      const __half* pbc = pb + j0 * kp;
+      uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)w, (uint64_t)ns};
+      uint64_t stridesb[2] = {(uint64_t)kp * 2, (uint64_t)b_plane * 2};
+      uint32_t boxb[3] = {64, (uint32_t)sp::BN, 1};
+      rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pbc, dimsb, stridesb, boxb,
+                        CU_TENSOR_MAP_SWIZZLE_128B);
+      if (rc) break;
+      uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
+      rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pbc, dimsb, stridesb, boxh,
+                        CU_TENSOR_MAP_SWIZZLE_128B);
+      if (rc) break;
+    }
+    p.n = w;
+    p.tiles_n = (int)ceil_div(w, sp::BN);
+    p.sbuf = sbuf + j0 * m;
+    {
+      KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, X);
+      int variant = 0;
+      ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, X, &variant);
+      if (ce != cudaSuccess) {
+        rc = cuda_fail(ce, "Ozaki slice launch");
+        break;
+      }
+      call_info().multicast = variant;
     }
     note_launch();
-    ce = cudaGetLastError();
-    if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki launch");
-    if ((rc = columns_done(g, j0, j1, s)) != 0) return rc;
+    // C's columns j0..j1: recombination; with C staged from host memory and
+    // one chunk, in column ranges each copied back while the next is computed
+    ce = defer_c ? cudaStreamWaitEvent(X, ev_c[c], 0) : wait_operand(g, 2, X);
+    if (ce != cudaSuccess) {
+      rc = cuda_fail(ce, "operand staging");
+      break;
+    }
+    const int64_t nsub = (nch == 1 && stg && stg->writeback) ? std::min<int64_t>(4, w) : 1;
+    for (int64_t q = 0; q < nsub && !rc; ++q) {
+      cp.j0 = j0 + w * q / nsub;
+      cp.j1 = j0 + w * (q + 1) / nsub;
+      const int64_t bx = ceil_div(m, 512);
+      const int64_t by =
+          std::min<int64_t>({cp.j1 - cp.j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
+      {
+        KernelTimer kt(MOMMS_KERNEL_COMBINE, X);
+        combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, X>>>(cp);
+      }
+      note_launch();
+      ce = cudaGetLastError();
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki launch");
+      if (!rc) rc = columns_done(g, cp.j0, cp.j1, X);
+    }
+  }
+  if (ev_fork) {
+    // s waits for the second stream's chunks (also after an error: the
+    // scratch freed below may still be in use there)
+    ce = cudaEventRecord(ev_join, ds->aux);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(s, ev_join, 0);
+    if (!rc && ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+    cudaEventDestroy(ev_fork);
+    cudaEventDestroy(ev_join);
   }
   if (planes_buf) cudaFreeAsync(planes_buf, s);
   cudaFreeAsync(sbuf, s);
   cudaFreeAsync(ebuf, s);
-  return MOMMS_OK;
+  return rc;
 }
 
 }  // namespace momms

@@ -70,6 +70,26 @@ int stage_copy_in(const momms_operand& op, size_t es, const Staged& st, cudaStre
   return MOMMS_OK;
 }
 
+// Host -> device copy of columns [j0, j1) of a plain-pitch view into its
+// staging buffer, on stream `s` (the mirror of stage_out_cols).
+int stage_in_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s) {
+  if (st.rows == 0 || j1 <= j0) return MOMMS_OK;
+  cudaError_t e;
+  if (st.row_major) {  // each row holds columns j0..j1 contiguously
+    e = cudaMemcpy2DAsync(static_cast<char*>(st.owned) + (size_t)j0 * es, (size_t)st.ld * es,
+                          static_cast<const char*>(op.ptr) + (size_t)j0 * es,
+                          (size_t)(st.rows == 1 ? st.cols : op.rs) * es, (size_t)(j1 - j0) * es, (size_t)st.rows,
+                          cudaMemcpyHostToDevice, s);
+  } else {  // columns j0..j1, each contiguous
+    e = cudaMemcpy2DAsync(static_cast<char*>(st.owned) + (size_t)j0 * st.ld * es, (size_t)st.ld * es,
+                          static_cast<const char*>(op.ptr) + (size_t)j0 * op.cs * es,
+                          (size_t)(st.cols == 1 ? st.rows : op.cs) * es, (size_t)st.rows * es, (size_t)(j1 - j0),
+                          cudaMemcpyHostToDevice, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "H2D copy");
+  return MOMMS_OK;
+}
+
 // Device -> host copy of columns [j0, j1) of a staged C whose host view has a
 // plain pitch (plain_pitch), on stream `s`.
 int stage_out_cols(const momms_operand& op, size_t es, const Staged& st, int64_t j0, int64_t j1, cudaStream_t s) {
@@ -114,8 +134,5 @@ int stage_out(const momms_operand& op, size_t es, const Staged& st, cudaStream_t
     }
   return MOMMS_OK;
 }
-
-// Per-call staging state: the hooks the launchers see, the copy stream and
-// events (0-2: A, B, C copied in; 3: buffers allocated; 4: copies done).
 
 }  // namespace momms
