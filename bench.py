@@ -447,10 +447,10 @@ def measure_out_of_core(lib, mg, torch, size=16384, budget_gib=4):
 
 def measure_packed(lib, mg, torch, sizes=(1024, 2048, 8192), reps=10):
     """Emulated FP64 calls on resident operands: per-call time unpacked (the
-    slice count sampled each call), with A and B packed once (8 slices, no
+    slice count sampled each call), with A and B packed once (7 slices, no
     pre-pass, no host round trip), and the packed call replayed from a CUDA
-    graph. Same results bit for bit as the unpacked call with 8 slices."""
-    out = {"workload": "emulated FP64 C = A*B (8 slices), m=n=k in " + "/".join(str(x) for x in sizes) +
+    graph. Same results bit for bit as the unpacked call with 7 slices."""
+    out = {"workload": "emulated FP64 C = A*B (7 slices), m=n=k in " + "/".join(str(x) for x in sizes) +
            ", device-resident operands; A and B packed once by momms_pack"}
     rows = []
     for size in sizes:
@@ -466,7 +466,7 @@ def measure_packed(lib, mg, torch, sizes=(1024, 2048, 8192), reps=10):
         for role, X in ((mg.ROLE_A, A), (mg.ROLE_B, B)):
             op = mg.Operand(X.data_ptr(), 1, size, mg.MEM_DEVICE, 0)
             h = ctypes.c_void_p()
-            mg.check(lib.momms_pack(mg.DTYPE_F64, mg.PREC_OZAKI, role, size, size, ctypes.byref(op), 8, sp,
+            mg.check(lib.momms_pack(mg.DTYPE_F64, mg.PREC_OZAKI, role, size, size, ctypes.byref(op), 0, sp,
                                     ctypes.byref(h)), lib)
             packs.append(h)
         dp = _desc(mg, size, size, size, packs[0].value, packs[1].value, C.data_ptr(), mg.MEM_DEVICE, mg.PREC_OZAKI)
@@ -612,7 +612,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64",
         "data": f"synthetic: uniform[-1,1] from seed {SEED}, column-major, C initialised like A and B",
         "config": {"workload": WORKLOAD.replace("8192", str(size)), "m": m, "n": n, "k": k,
-                   "precision": "emulated FP64 (Ozaki: 7-bit fp16 digit slices on tcgen05, exact int32 "
+                   "precision": "emulated FP64 (Ozaki: 8-bit digit slices as fp16 on tcgen05, exact int32 "
                                 "digit sums, FP64 recombination); slice count chosen per call for the "
                                 "default FP64-level target",
                    "slices": info.slices, "slice_products": info.pairs,

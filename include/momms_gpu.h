@@ -147,9 +147,10 @@ int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, co
  *
  * role: MOMMS_ROLE_A (rows x cols = m x k) or MOMMS_ROLE_B (k x n); the pack
  * fits only that position and those sizes. src: host or device view (AUTO /
- * HOST / DEVICE). slices: OZAKI only, 1..16 (0 = 8, the count the FP64-level
- * target takes for operands without a wide exponent spread). Emulated calls
- * with k > 65536 cannot use packed operands (their k slabs re-scale per slab).
+ * HOST / DEVICE). slices: OZAKI only, 1..16 (0 = 7 slices of 8 bits, the
+ * count the FP64-level target takes for operands without a wide exponent
+ * spread). Emulated calls with k > 32704 cannot use packed operands (their k
+ * slabs re-scale per slab).
  * Synchronous; the pack owns its device memory until momms_packed_destroy. */
 typedef enum { MOMMS_ROLE_A = 0, MOMMS_ROLE_B = 1 } momms_role;
 typedef struct momms_packed_s* momms_packed;

@@ -132,6 +132,13 @@ __device__ __forceinline__ uint32_t mapa_shared(const void* p, uint32_t rank) {
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
 }
+// Arrival without release semantics: for signals that order no memory
+// accesses of this thread (a drained TMEM buffer: tcgen05.wait::ld has
+// already completed its reads). A release at cluster scope would first wait
+// for this thread's earlier global and local stores.
+__device__ __forceinline__ void mbar_arrive_cluster_relaxed(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
 
 // ---- thread-block clusters ----
 __device__ __forceinline__ uint32_t cluster_ctarank() {

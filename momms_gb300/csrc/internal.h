@@ -187,6 +187,9 @@ int gemm_streamed(const momms_gemm_desc& d, const bool host[3], const BlockPlan&
 int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s);
 int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s);
 int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s);
+// Longest k of one emulated launch (8-bit digits: 511 k-blocks of 64 keep a
+// digit pair's int32 sum exact); longer k runs in slabs accumulated into C.
+constexpr int64_t kOzakiMaxK = 32704;
 // Ozaki FP64 emulation: target relative error (0 = FP64 level) and slice count
 // (0 = chosen from the target). *slices_used receives the count actually used.
 int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int* slices_used, cudaStream_t s);

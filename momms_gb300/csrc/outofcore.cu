@@ -34,7 +34,6 @@ constexpr int64_t kGran = 256;         // block sizes are multiples of the 128 x
 constexpr double kPlanSms = 152.0;
 constexpr double kHostBw = 2.0e11;
 constexpr double kLaunchS = 3e-5;
-constexpr int64_t kOzakiMaxK = 65536;  // one Ozaki launch: int32 digit sums over k <= 2^16
 
 size_t esize(int dtype) { return dtype == MOMMS_DTYPE_F64 ? 8 : 4; }
 
@@ -78,10 +77,10 @@ size_t work_bytes(int dtype, int precision, int slices, int64_t m, int64_t n, in
   const double M = (double)m, N = (double)n, K = (double)k;
   double bytes;
   if (precision == MOMMS_PREC_OZAKI) {
-    const int s = slices > 0 ? slices : 9;  // FP64-level targets take up to 9 slices
+    const int s = slices > 0 ? slices : 8;  // FP64-level targets take up to 8 slices
     // digit planes of A and B, one int32 sum plane per accumulation group
     const double groups = (double)ozaki_group_count(s, k);
-    bytes = 2.0 * s * (M + N) * (double)round_up(std::min<int64_t>(k, 65536), 8) + 4.0 * groups * M * N +
+    bytes = 2.0 * s * (M + N) * (double)round_up(std::min<int64_t>(k, kOzakiMaxK), 8) + 4.0 * groups * M * N +
             12.0 * (M + N);
   } else if (precision == MOMMS_PREC_SPLIT_TF32) {
     bytes = 8.0 * (M + N) * (double)round_up(k, 4);

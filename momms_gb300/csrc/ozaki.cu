@@ -8,14 +8,17 @@
 // wide-enough accumulator. Products on the same anti-diagonal d = t + u share
 // the weight 2^(-bits*d); the scheme keeps d <= s + 1 (triangular truncation).
 //
-// GB300 form (sm_103a has no integer tcgen05 kind): digits are fp16 values
-// (exact for |d| <= 2048), the products run on tcgen05 kind::f16 with FP32
-// accumulation in TMEM, and every accumulation chunk is kept below 2^22 so
-// that it is an exact integer; chunks are gathered in int32 registers, and the
-// diagonals are combined in FP64 by Horner's rule in the epilogue
-// (R = S_d + 2^-bits R, from the smallest weight up), so FP64 arithmetic is
-// used only for the exponent scaling and this recombination. See
-// slicegemm.cuh for the engine.
+// GB300 form (sm_103a has no integer tcgen05 kind): digits are 8-bit integers
+// held as fp16 values (exact for |d| <= 2048), the products run on tcgen05
+// kind::f16 with FP32 accumulation in TMEM, and every accumulation chunk's
+// sum of absolute products is kept at or below 2^24, so that every partial
+// sum is an exactly representable integer; chunks are gathered in int32
+// registers, and the diagonals are combined exactly in 128-bit integers
+// (Horner's rule over the diagonals) and rounded once to FP64. See
+// slicegemm.cuh for the engine. With 8-bit digits 7 slices cover 56 bits with
+// 28 slice products, where 7-bit digits need 8 slices and 36 products; the
+// price is 4x larger products, so TMEM is drained every 4 (top x top), 8 (top
+// x centred) or 16 (centred x centred) k-blocks.
 //
 // The slice count is chosen per call from the requested componentwise error
 // (|dC_ij| / (|A||B|)_ij) with a bound evaluated on sampled entries: with RN
@@ -38,8 +41,18 @@ namespace momms {
 
 namespace {
 
-constexpr int kDigitBits = 7;
-constexpr int64_t kMaxK = 65536;  // k per launch: int32 digit sums stay exact up to 2^16 products
+constexpr int kDigitBits = 8;
+// k per launch (kOzakiMaxK): the largest product of two digits is 2^16, so a
+// single pair's int32 sum stays below 2^31 for up to 511 k-blocks of 64
+constexpr int64_t kMaxK = kOzakiMaxK;
+static_assert((kMaxK / 64) * 64 * (1ll << (2 * kDigitBits)) < (1ll << 31), "int32 digit sums must stay exact");
+// Horner levels combined exactly: with at most 16 groups of |S| < 2^31 per
+// level, R stays below 2^(36 + bits*dmax) < 2^127
+constexpr int kHornerLevels = (127 - 36) / kDigitBits;
+// an int32 group sum's bound (sums of the pairs' worst cases)
+constexpr double kGroupLimit = 2147483647.0;
+// one TMEM chunk's bound: integers up to 2^24 are exact in FP32
+constexpr double kChunkBound = 16777216.0;
 
 // Everything in the pre-pass runs on integer bit patterns: GB300's FP64 pipe
 // is about 1 TFLOP/s, so FP64 arithmetic per element would dominate.
@@ -139,10 +152,11 @@ __device__ __forceinline__ U offset_digits(double v, int e) {
 
 // Digit planes of an operand for NS slices: plane t holds digit position
 // NS-1-t of every element (plane 0 the top digit), sign applied, as fp16.
-// A pair of digits d0, d1 in [-128, 128] becomes one __half2 without a
+// A pair of digits d0, d1 in [-2^bits, 2^bits] becomes one __half2 without a
 // conversion instruction: the fp16 bit patterns 0x6400 + u are the integers
-// 1024 + u (u < 1024), so packing u = d + 128 under 0x6400 and subtracting
-// 1152 gives d exactly (and +0 for d = 0, as an integer conversion does).
+// 1024 + u (u < 1024), so packing u = d + 2^bits under 0x6400 and subtracting
+// 1024 + 2^bits gives d exactly (and +0 for d = 0, as an integer conversion
+// does).
 template <int NS>
 struct OzakiSliceOp {
   using Tout = __half;
@@ -154,7 +168,9 @@ struct OzakiSliceOp {
     const int e = exps[r];
     const U Y0 = offset_digits<NS, U>(v0, e), Y1 = offset_digits<NS, U>(v1, e);
     const bool n0 = __double_as_longlong(v0) < 0, n1 = __double_as_longlong(v1) < 0;
-    const __half2 bias = __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480));  // 1152
+    static_assert(2 * (1 << bits) < 1024, "digits must fit the 0x6400 pattern");
+    constexpr unsigned short kBias = 0x6400 + (1u << bits);  // 1024 + 2^bits
+    const __half2 bias = __halves2half2(__ushort_as_half(kBias), __ushort_as_half(kBias));
     // least significant position first, into the last plane, walking back
     U y0 = Y0, y1 = Y1;
     __half* o = out + (int64_t)(NS - 1) * plane_elems;
@@ -170,7 +186,7 @@ struct OzakiSliceOp {
         y0 >>= bits;
         y1 >>= bits;
       }
-      const unsigned u0 = (unsigned)((n0 ? -d0 : d0) + 128), u1 = (unsigned)((n1 ? -d1 : d1) + 128);
+      const unsigned u0 = (unsigned)((n0 ? -d0 : d0) + (1 << bits)), u1 = (unsigned)((n1 ? -d1 : d1) + (1 << bits));
       const unsigned w = 0x64006400u | u0 | (u1 << 16);
       *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
       o -= plane_elems;
@@ -582,25 +598,60 @@ int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
   return rc;
 }
 
-int ozaki_group_count(int ns, int64_t k) {
-  // the launcher's schedule below: one group per diagonal d = t + u, split
-  // where a diagonal's int32 sums could pass 2^30
+namespace {
+// The slice-product schedule for ns slices over k: diagonals d = t + u from
+// the smallest weight (d = ns+1) to the largest (d = 2), each diagonal's pairs
+// (t, d-t) in t order, cut into accumulation groups whose worst-case int32
+// sums (k * 2^bits_t * 2^bits_u over the group's pairs; the top digit has
+// `bits` bits, the centred ones bits-1) stay within kGroupLimit. A group's
+// TMEM chunk keeps one chunk's sum within kChunkBound for its largest product.
+struct Schedule {
+  int np = 0, ng = 0;
+  uint8_t pair_a[sp::MAX_PAIRS], pair_b[sp::MAX_PAIRS];
+  int group_begin[sp::MAX_GROUPS + 1];
+  int chunk_kb[sp::MAX_GROUPS];
+  uint8_t level[sp::MAX_GROUPS];  // d - 2
+};
+
+bool ozaki_schedule(int ns, int64_t k, Schedule* sc) {
   const int bits = kDigitBits;
-  const double kblocks = (double)ceil_div(std::min<int64_t>(std::max<int64_t>(k, 1), kMaxK), 64);
-  int ng = 0;
-  for (int d = 2; d <= ns + 1; ++d) {
-    int nt = 0;
-    double maxprod = 0.0;
+  const int64_t kblocks = ceil_div(std::min<int64_t>(std::max<int64_t>(k, 1), kMaxK), 64);
+  const double kspan = (double)kblocks * 64.0;
+  auto prod = [&](int t, int u) { return ldexp(1.0, (t == 1 ? bits : bits - 1) + (u == 1 ? bits : bits - 1)); };
+  sc->np = sc->ng = 0;
+  for (int d = ns + 1; d >= 2; --d) {
+    double gsum = 0.0, gmax = 0.0;
+    bool open = false;
     for (int t = 1; t <= ns; ++t) {
       const int u = d - t;
       if (u < 1 || u > ns) continue;
-      ++nt;
-      maxprod = fmax(maxprod, ldexp(1.0, t == 1 ? bits : bits - 1) * ldexp(1.0, u == 1 ? bits : bits - 1));
+      const double pb = prod(t, u);
+      if (open && gsum + kspan * pb > kGroupLimit) open = false;  // this pair starts the next group
+      if (!open) {
+        if (sc->ng >= sp::MAX_GROUPS) return false;
+        sc->group_begin[sc->ng] = sc->np;
+        sc->level[sc->ng] = (uint8_t)(d - 2);
+        ++sc->ng;
+        gsum = gmax = 0.0;
+        open = true;
+      }
+      if (sc->np >= sp::MAX_PAIRS) return false;
+      sc->pair_a[sc->np] = (uint8_t)(t - 1);
+      sc->pair_b[sc->np] = (uint8_t)(u - 1);
+      ++sc->np;
+      gsum += kspan * pb;
+      gmax = fmax(gmax, pb);
+      sc->chunk_kb[sc->ng - 1] = (int)std::max<int64_t>(1, (int64_t)(kChunkBound / gmax) / 64);
     }
-    const int ppg = (int)std::max(1.0, floor(ldexp(1.0, 30) / (kblocks * 64.0 * maxprod)));
-    ng += (nt + ppg - 1) / ppg;
   }
-  return ng;
+  sc->group_begin[sc->ng] = sc->np;
+  return true;
+}
+}  // namespace
+
+int ozaki_group_count(int ns, int64_t k) {
+  Schedule sc;
+  return ozaki_schedule(ns, k, &sc) ? sc.ng : sp::MAX_GROUPS;
 }
 
 namespace {
@@ -631,8 +682,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   if (g.k > kMaxK) {
     if (g.pk[0] || g.pk[1])
-      return fail(MOMMS_ERR_UNSUPPORTED, "packed operands need k <= 65536 (longer k runs in re-scaled slabs)");
-    // k slabs of at most 2^16 (the int32 digit sums' range), later slabs
+      return fail(MOMMS_ERR_UNSUPPORTED, "packed operands need k <= %lld (longer k runs in re-scaled slabs)",
+                  (long long)kMaxK);
+    // k slabs of at most kMaxK (the int32 digit sums' range), later slabs
     // accumulating into C with beta = 1 like the reference's PartK
     // (src/composables/part.rs:96-110); each slab meets the target on its own
     const int64_t nslab = ceil_div(g.k, kMaxK), kb = round_up(ceil_div(g.k, nslab), 64);
@@ -764,7 +816,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const __half* pb = PB ? static_cast<const __half*>(PB->planes) : planes_buf + (PA ? 0 : (size_t)ns * a_plane);
   if (!PA) ozaki_operand_planes(ns, A, g.a.rs, g.a.cs, m, k, const_cast<__half*>(pa), kp, rexp, s);
 
-  if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= 65536 per launch");
+  if (k > kMaxK) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation supports k <= %lld per launch", (long long)kMaxK);
   CUtensorMap tmA;
   {
     uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)ns};
@@ -782,43 +834,15 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   p.tiles_m = (int)ceil_div(m, sp::BM);
   CombineParams cp;
   memset(&cp, 0, sizeof(cp));
-  uint8_t dgrp[sp::MAX_GROUPS];  // level (d - 2) of each group
-  // Diagonals from the smallest weight (d = ns+1) to the largest (d = 2). A
-  // diagonal whose int32 sums could pass 2^30 is split into several groups
-  // of whole pairs; only the first group of a diagonal shifts R by 2^-bits.
-  int np = 0, ng = 0;
-  for (int gi = 0; gi < ns; ++gi) {
-    const int d = ns + 1 - gi;  // digit indices t, u in 1..ns with t + u = d
-    int tlist[16], nt = 0;
-    double maxprod = 0.0;
-    for (int t = 1; t <= ns; ++t) {
-      const int u = d - t;
-      if (u < 1 || u > ns) continue;
-      tlist[nt++] = t;
-      const double bt = ldexp(1.0, t == 1 ? bits : bits - 1), bu = ldexp(1.0, u == 1 ? bits : bits - 1);
-      maxprod = fmax(maxprod, bt * bu);
-    }
-    // every TMEM chunk keeps |sum| <= 2^22 (exact in FP32, and inside the
-    // magic-constant conversion range)
-    const int chunk = (int)std::max<int64_t>(1, (int64_t)(ldexp(1.0, 22) / maxprod) / p.kelems);
-    // pairs per group so that the int32 group sums stay below 2^30
-    const double per_pair = (double)p.kblocks * p.kelems * maxprod;
-    const int pairs_per_group = (int)std::max(1.0, floor(ldexp(1.0, 30) / per_pair));
-    for (int i0 = 0; i0 < nt; i0 += pairs_per_group) {
-      if (ng >= sp::MAX_GROUPS) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
-      p.group_begin[ng] = np;
-      p.chunk_kb[ng] = chunk;
-      dgrp[ng] = (uint8_t)(d - 2);
-      for (int i = i0; i < std::min(nt, i0 + pairs_per_group); ++i) {
-        p.pair_a[np] = (uint8_t)(tlist[i] - 1);
-        p.pair_b[np] = (uint8_t)(d - tlist[i] - 1);
-        ++np;
-      }
-      ++ng;
-    }
-  }
+  Schedule sch;
+  if (!ozaki_schedule(ns, k, &sch)) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
+  const int np = sch.np, ng = sch.ng;
+  const uint8_t* dgrp = sch.level;
+  memcpy(p.pair_a, sch.pair_a, (size_t)np);
+  memcpy(p.pair_b, sch.pair_b, (size_t)np);
+  memcpy(p.group_begin, sch.group_begin, sizeof(int) * (size_t)(ng + 1));
+  memcpy(p.chunk_kb, sch.chunk_kb, sizeof(int) * (size_t)ng);
   p.ngroups = ng;
-  p.group_begin[ng] = np;
   call_info().slices = ns;
   call_info().pairs = np;
   call_info().groups = ng;
@@ -835,7 +859,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   {
     // Horner entries in level order: a shift by one level between levels
     // (an empty level only shifts), then each group of the level
-    const int dmax = std::min(ns - 1, 12);
+    const int dmax = std::min(ns - 1, kHornerLevels);
     int nh = 0;
     for (int L = 0; L <= dmax; ++L) {
       bool first = true;
@@ -857,7 +881,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     for (int gi = 0; gi < ng; ++gi)
       if (dgrp[gi] > dmax) {
         cp.tail_g[cp.ntail] = (uint8_t)gi;
-        cp.tail_sh[cp.ntail] = (uint8_t)(bits * (dgrp[gi] - dmax));
+        // floor(S / 2^sh); for |S| < 2^31 a shift by 31 already gives it
+        cp.tail_sh[cp.ntail] = (uint8_t)std::min(31, bits * (dgrp[gi] - dmax));
         ++cp.ntail;
       }
     cp.scale_off = -2 * bits - bits * dmax;

@@ -85,8 +85,8 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
   // k is the operand's inner dimension: A's columns, B's rows
   const int64_t K = role == MOMMS_ROLE_A ? cols : rows;
   const int64_t R = role == MOMMS_ROLE_A ? rows : cols;
-  if (precision == MOMMS_PREC_OZAKI && K > 65536)
-    return fail(MOMMS_ERR_UNSUPPORTED, "packed emulated operands need k <= 65536");
+  if (precision == MOMMS_PREC_OZAKI && K > kOzakiMaxK)
+    return fail(MOMMS_ERR_UNSUPPORTED, "packed emulated operands need k <= %lld", (long long)kOzakiMaxK);
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -124,7 +124,7 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
       rc = repack_colmajor(v, rows, cols, es, p->data, p->ld, s);
     }
   } else if (precision == MOMMS_PREC_OZAKI) {
-    p->np = slices > 0 ? slices : 8;
+    p->np = slices > 0 ? slices : 7;  // 56 bits: FP64 level for most data
     p->kp = round_up(K, 8);
     const size_t plane_bytes = (size_t)p->np * (size_t)R * (size_t)p->kp * 2;
     const size_t exps_off = round_up((int64_t)plane_bytes, 256);

@@ -26,8 +26,10 @@
 //               (round to nearest) and C = alpha*sum + beta*C is written at
 //               the end of the tile. Used by the split-TF32 f32 path (pairs
 //               lo*hi, hi*lo, hi*hi).
-//   EPI_OZAKI : integer-valued slices; every chunk is exact in FP32 and is
-//               added into int32 accumulators; at the end of each group the
+//   EPI_OZAKI : integer-valued slices; every chunk is exact in FP32 (the
+//               host sizes chunks so that sums of absolute products stay
+//               within 2^24) and is converted and added into int32
+//               accumulators; at the end of each group the
 //               exact sums are written to that group's int32 plane (the FP64
 //               recombination runs afterwards in its own kernel, so no FP64
 //               work sits in this pipeline).
@@ -99,10 +101,31 @@ __device__ __forceinline__ void tile_coords(int64_t t, int tiles_m, int tiles_n,
   tn = (int)(r / gm);
 }
 
-// f32 integer value |x| <= 2^22 -> int32 via the 1.5*2^23 magic constant
-__device__ __forceinline__ int f2i_exact(uint32_t bits) {
-  const float f = __uint_as_float(bits) + 12582912.0f;
-  return (int)(__float_as_uint(f) - 0x4B400000u);
+// Accumulators of drained chunks: Ozaki sums are int32 (each chunk value is
+// an integer of magnitude <= 2^24, exact in FP32, converted exactly);
+// split-TF32 sums are FP32.
+template <int EPI>
+using EpiAcc = typename std::conditional<EPI == EPI_OZAKI, int, float>::type;
+
+// Drains one TMEM chunk (this thread's row, NC columns from taddr) into S.
+// The loads run one 16-column batch ahead of the adds: a batch's wait comes
+// after the previous batch's adds.
+template <int EPI, int NC>
+__device__ __forceinline__ void drain_chunk(uint32_t taddr, EpiAcc<EPI> (&S)[NC]) {
+  uint32_t ra[16], rb[16];
+  tc::ld16(taddr, ra);
+#pragma unroll
+  for (int pc = 0; pc < NC / 16; ++pc) {
+    uint32_t(&cur)[16] = (pc & 1) ? rb : ra;
+    uint32_t(&nxt)[16] = (pc & 1) ? ra : rb;
+    tc::ld_wait(cur);
+    if (pc + 1 < NC / 16) tc::ld16(taddr + (pc + 1) * 16, nxt);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (EPI == EPI_OZAKI) S[pc * 16 + j] += __float2int_rz(__uint_as_float(cur[j]));
+      else S[pc * 16 + j] += __uint_as_float(cur[j]);
+    }
+  }
 }
 
 template <int KIND, int EPI, bool MC>
@@ -303,10 +326,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       // per-thread accumulators of finished chunks: exact int32 digit sums
       // (Ozaki) or FP32 sums rounded to nearest (split-TF32), which keeps the
       // tensor core's internal accumulation to one chunk at a time
-      typedef typename std::conditional<EPI == EPI_OZAKI, int, float>::type Acc;
-      Acc S[EPI_COLS];
+      EpiAcc<EPI> S[EPI_COLS];
 #pragma unroll
-      for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+      for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
         const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
         const int chunk = p.chunk_kb[g];
@@ -318,17 +340,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           tc::fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-#pragma unroll
-          for (int pc = 0; pc < EPI_COLS / 16; ++pc) {
-            uint32_t r[16];
-            tc::ld16(taddr + pc * 16, r);
-            tc::ld_wait();
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              if (EPI == EPI_OZAKI) S[pc * 16 + j] += f2i_exact(r[j]);
-              else S[pc * 16 + j] += __uint_as_float(r[j]);
-            }
-          }
+          drain_chunk<EPI, EPI_COLS>(taddr, S);
           tc::fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
@@ -342,11 +354,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) {
               const int64_t col = col0 + j;
-              if (col < p.n) srow[col * p.m] = (int)S[j];
+              if (col < p.n) srow[col * p.m] = S[j];
             }
           }
 #pragma unroll
-          for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+          for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
         }
       }
       if (EPI == EPI_F32 && row < p.m) {
@@ -573,10 +585,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       coords(t % tile_units, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
-      typedef typename std::conditional<EPI == EPI_OZAKI, int, float>::type Acc;
-      Acc S[EPI_COLS];
+      EpiAcc<EPI> S[EPI_COLS];
 #pragma unroll
-      for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+      for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
         const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
         const int chunk = p.chunk_kb[g];
@@ -588,20 +599,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           tc::fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-#pragma unroll
-          for (int pc = 0; pc < EPI_COLS / 16; ++pc) {
-            uint32_t r[16];
-            tc::ld16(taddr + pc * 16, r);
-            tc::ld_wait();
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              if (EPI == EPI_OZAKI) S[pc * 16 + j] += f2i_exact(r[j]);
-              else S[pc * 16 + j] += __uint_as_float(r[j]);
-            }
-          }
+          drain_chunk<EPI, EPI_COLS>(taddr, S);
           tc::fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive_cluster(tempty_leader[buf]);
+          if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
           acc_ph[buf] ^= 1;
           buf ^= 1;
         }
@@ -611,11 +612,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) {
               const int64_t col = col0 + j;
-              if (col < p.n) srow[col * p.m] = (int)S[j];
+              if (col < p.n) srow[col * p.m] = S[j];
             }
           }
 #pragma unroll
-          for (int j = 0; j < EPI_COLS; ++j) S[j] = Acc(0);
+          for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
         }
       }
       if (EPI == EPI_F32 && row < p.m) {

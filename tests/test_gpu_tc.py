@@ -80,12 +80,41 @@ def test_ozaki_integer_data_is_exact(gpu):
 
 
 def test_ozaki_two_digit_integers_exact(gpu):
-    """Entries up to 2^12 need two 7-bit digits; with s = 3 the kept pairs
+    """Entries up to 2^12 need at most two digits; with s = 3 the kept pairs
     (t + u <= 4) include every nonzero product, so the result is exact."""
     rng = np.random.default_rng(2)
     m, n, k = 129, 257, 700
     A = np.asfortranarray(rng.integers(-4000, 4001, (m, k)).astype(np.float64))
     B = np.asfortranarray(rng.integers(-4000, 4001, (k, n)).astype(np.float64))
+    C0 = np.zeros((m, n), order="F")
+    C = gu.gemm_device(gpu, A, B, C0, 1.0, 0.0, precision=mg.PREC_OZAKI, slices=3)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    assert np.array_equal(C, exact)
+
+
+def test_ozaki_full_digit_chunks_exact(gpu):
+    """One 8-bit digit per entry (values 200..255, one sign): every TMEM
+    chunk of the top x top pair (4 k-blocks of 64) sums to within 1 % of
+    the 2^24 bound with arbitrary low bits; the result must be exact."""
+    rng = np.random.default_rng(12)
+    m, n, k = 256, 320, 8192
+    A = np.asfortranarray(rng.integers(200, 256, (m, k)).astype(np.float64))
+    B = np.asfortranarray(rng.integers(200, 256, (k, n)).astype(np.float64))
+    C0 = np.zeros((m, n), order="F")
+    C = gu.gemm_device(gpu, A, B, C0, 1.0, 0.0, precision=mg.PREC_OZAKI, slices=1)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    assert np.array_equal(C, exact)
+
+
+def test_ozaki_top_by_centred_chunks_exact(gpu):
+    """Values 256 t + 128 (t in 200..254) split into a top digit t + 1 and a
+    centred digit -128: the top x centred chunks (8 k-blocks) reach 99.6 %
+    of the 2^24 bound, all of one sign; with 3 slices every nonzero digit
+    product is kept, so the result must be exact."""
+    rng = np.random.default_rng(13)
+    m, n, k = 192, 256, 4096
+    A = np.asfortranarray((256 * rng.integers(200, 255, (m, k)) + 128).astype(np.float64))
+    B = np.asfortranarray((256 * rng.integers(200, 255, (k, n)) + 128).astype(np.float64))
     C0 = np.zeros((m, n), order="F")
     C = gu.gemm_device(gpu, A, B, C0, 1.0, 0.0, precision=mg.PREC_OZAKI, slices=3)
     exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
