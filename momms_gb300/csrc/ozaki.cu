@@ -604,12 +604,13 @@ namespace {
 // (t, d-t) in t order, cut into accumulation groups whose worst-case int32
 // sums (k * 2^bits_t * 2^bits_u over the group's pairs; the top digit has
 // `bits` bits, the centred ones bits-1) stay within kGroupLimit. A group's
-// TMEM chunk keeps one chunk's sum within kChunkBound for its largest product.
+// Each pair's TMEM chunks keep one chunk's sum within kChunkBound for that
+// pair's largest digit product (4, 8 or 16 k-blocks of 64 for 8-bit digits).
 struct Schedule {
   int np = 0, ng = 0;
   uint8_t pair_a[sp::MAX_PAIRS], pair_b[sp::MAX_PAIRS];
   int group_begin[sp::MAX_GROUPS + 1];
-  int chunk_kb[sp::MAX_GROUPS];
+  int pair_chunk[sp::MAX_PAIRS];
   uint8_t level[sp::MAX_GROUPS];  // d - 2
 };
 
@@ -620,7 +621,7 @@ bool ozaki_schedule(int ns, int64_t k, Schedule* sc) {
   auto prod = [&](int t, int u) { return ldexp(1.0, (t == 1 ? bits : bits - 1) + (u == 1 ? bits : bits - 1)); };
   sc->np = sc->ng = 0;
   for (int d = ns + 1; d >= 2; --d) {
-    double gsum = 0.0, gmax = 0.0;
+    double gsum = 0.0;
     bool open = false;
     for (int t = 1; t <= ns; ++t) {
       const int u = d - t;
@@ -632,16 +633,15 @@ bool ozaki_schedule(int ns, int64_t k, Schedule* sc) {
         sc->group_begin[sc->ng] = sc->np;
         sc->level[sc->ng] = (uint8_t)(d - 2);
         ++sc->ng;
-        gsum = gmax = 0.0;
+        gsum = 0.0;
         open = true;
       }
       if (sc->np >= sp::MAX_PAIRS) return false;
       sc->pair_a[sc->np] = (uint8_t)(t - 1);
       sc->pair_b[sc->np] = (uint8_t)(u - 1);
+      sc->pair_chunk[sc->np] = (int)std::max<int64_t>(1, (int64_t)(kChunkBound / pb) / 64);
       ++sc->np;
       gsum += kspan * pb;
-      gmax = fmax(gmax, pb);
-      sc->chunk_kb[sc->ng - 1] = (int)std::max<int64_t>(1, (int64_t)(kChunkBound / gmax) / 64);
     }
   }
   sc->group_begin[sc->ng] = sc->np;
@@ -841,7 +841,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   memcpy(p.pair_a, sch.pair_a, (size_t)np);
   memcpy(p.pair_b, sch.pair_b, (size_t)np);
   memcpy(p.group_begin, sch.group_begin, sizeof(int) * (size_t)(ng + 1));
-  memcpy(p.chunk_kb, sch.chunk_kb, sizeof(int) * (size_t)ng);
+  memcpy(p.pair_chunk, sch.pair_chunk, sizeof(int) * (size_t)np);
   p.ngroups = ng;
   call_info().slices = ns;
   call_info().pairs = np;

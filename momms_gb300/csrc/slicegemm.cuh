@@ -4,7 +4,7 @@
 //   for each output tile (persistent, one CTA per SM, 128 x 256 tiles):
 //     for each group g (processed in order):
 //       S_g = sum over pairs (a, b) in g of  A_plane[a] * B_plane[b]^T
-//       accumulated in TMEM in chunks of at most chunk_kb k-blocks; each
+//       accumulated in TMEM, each pair in chunks of pair_chunk k-blocks; each
 //       finished chunk is handed to the epilogue (ping-pong TMEM buffers)
 //
 // Planes are K-major in HBM ([plane][row][k], k contiguous) and are loaded by
@@ -73,7 +73,7 @@ struct Params {
   int ngroups;
   int gchunk;  // groups per work unit: a tile's groups may run as separate units (0 = all)
   int group_begin[MAX_GROUPS + 1];
-  int chunk_kb[MAX_GROUPS];
+  int pair_chunk[MAX_PAIRS];  // k-blocks per TMEM accumulation chunk of each pair
   uint8_t pair_a[MAX_PAIRS], pair_b[MAX_PAIRS];
   // EPI_F32
   float alpha_f, beta_f;
@@ -262,42 +262,44 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t t = unit_at(r);
         if (t >= units) continue;
         for (int g = g_begin(t); g < g_end(t); ++g) {
-          const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
-          const int chunk = p.chunk_kb[g];
-          for (int s0 = 0; s0 < total; s0 += chunk) {
-            if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-              report_status(p.status, DEV_TIMEOUT_TMEM);
-              *abort_flag = 1;
-              goto mma_done;
-            }
-            tc::fence_after();
-            const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-            const int s1 = min(total, s0 + chunk);
-            for (int st = s0; st < s1; ++st) {
-              if (!mbar_wait_bounded(&full[stage], ph)) {
-                report_status(p.status, DEV_TIMEOUT_FULL);
+          for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
+            const int total = p.kblocks;
+            const int chunk = p.pair_chunk[pp];
+            for (int s0 = 0; s0 < total; s0 += chunk) {
+              if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+                report_status(p.status, DEV_TIMEOUT_TMEM);
                 *abort_flag = 1;
                 goto mma_done;
               }
               tc::fence_after();
-              const uint32_t a_addr = smem_u32(smem + stage * STAGE_BYTES);
-              const uint32_t b_addr = a_addr + A_TILE;
+              const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+              const int s1 = min(total, s0 + chunk);
+              for (int st = s0; st < s1; ++st) {
+                if (!mbar_wait_bounded(&full[stage], ph)) {
+                  report_status(p.status, DEV_TIMEOUT_FULL);
+                  *abort_flag = 1;
+                  goto mma_done;
+                }
+                tc::fence_after();
+                const uint32_t a_addr = smem_u32(smem + stage * STAGE_BYTES);
+                const uint32_t b_addr = a_addr + A_TILE;
 #pragma unroll
-              for (int kk = 0; kk < KSTEPS; ++kk)
-                tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
-                              (st > s0 || kk > 0) ? 1u : 0u);
-              if (MC)
-                tc::commit_mc(&empty[stage], (uint16_t)0x3);  // both CTAs' copies of the stage are free
-              else
-                tc::commit(&empty[stage]);
-              if (++stage == STAGES) {
-                stage = 0;
-                ph ^= 1;
+                for (int kk = 0; kk < KSTEPS; ++kk)
+                  tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
+                                (st > s0 || kk > 0) ? 1u : 0u);
+                if (MC)
+                  tc::commit_mc(&empty[stage], (uint16_t)0x3);  // both CTAs' copies of the stage are free
+                else
+                  tc::commit(&empty[stage]);
+                if (++stage == STAGES) {
+                  stage = 0;
+                  ph ^= 1;
+                }
               }
+              tc::commit(&tfull[buf]);
+              acc_ph[buf] ^= 1;
+              buf ^= 1;
             }
-            tc::commit(&tfull[buf]);
-            acc_ph[buf] ^= 1;
-            buf ^= 1;
           }
         }
       }
@@ -330,22 +332,24 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
-        const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
-        const int chunk = p.chunk_kb[g];
-        for (int s0 = 0; s0 < total; s0 += chunk) {
-          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-            report_status(p.status, DEV_TIMEOUT_MMA);
-            *abort_flag = 1;
-            goto epi_done;
+        for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
+          const int total = p.kblocks;
+          const int chunk = p.pair_chunk[pp];
+          for (int s0 = 0; s0 < total; s0 += chunk) {
+            if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+              report_status(p.status, DEV_TIMEOUT_MMA);
+              *abort_flag = 1;
+              goto epi_done;
+            }
+            tc::fence_after();
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+            drain_chunk<EPI, EPI_COLS>(taddr, S);
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
           }
-          tc::fence_after();
-          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-          drain_chunk<EPI, EPI_COLS>(taddr, S);
-          tc::fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[buf]);
-          acc_ph[buf] ^= 1;
-          buf ^= 1;
         }
         if (EPI == EPI_OZAKI) {
           // end of group g: publish the exact int32 sums (column-major plane g)
@@ -528,39 +532,41 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t t = unit_at(r);
         if (t >= units) continue;
         for (int g = g_begin(t); g < g_end(t); ++g) {
-          const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
-          const int chunk = p.chunk_kb[g];
-          for (int s0 = 0; s0 < total; s0 += chunk) {
-            if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-              report_status(p.status, DEV_TIMEOUT_TMEM);
-              *abort_flag = 1;
-              goto mma_done;
-            }
-            tc::fence_after();
-            const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-            const int s1 = min(total, s0 + chunk);
-            for (int st = s0; st < s1; ++st) {
-              if (!mbar_wait_bounded(&full[stage], ph)) {
-                report_status(p.status, DEV_TIMEOUT_FULL);
+          for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
+            const int total = p.kblocks;
+            const int chunk = p.pair_chunk[pp];
+            for (int s0 = 0; s0 < total; s0 += chunk) {
+              if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+                report_status(p.status, DEV_TIMEOUT_TMEM);
                 *abort_flag = 1;
                 goto mma_done;
               }
               tc::fence_after();
-              const uint32_t a_addr = smem_u32(smem + stage * P_STAGE_BYTES);
-              const uint32_t b_addr = a_addr + A_TILE;
+              const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+              const int s1 = min(total, s0 + chunk);
+              for (int st = s0; st < s1; ++st) {
+                if (!mbar_wait_bounded(&full[stage], ph)) {
+                  report_status(p.status, DEV_TIMEOUT_FULL);
+                  *abort_flag = 1;
+                  goto mma_done;
+                }
+                tc::fence_after();
+                const uint32_t a_addr = smem_u32(smem + stage * P_STAGE_BYTES);
+                const uint32_t b_addr = a_addr + A_TILE;
 #pragma unroll
-              for (int kk = 0; kk < KSTEPS; ++kk)
-                tc::mma2<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
-                               (st > s0 || kk > 0) ? 1u : 0u);
-              tc::commit2_mc(&empty[stage], (uint16_t)0x3);
-              if (++stage == PSTAGES) {
-                stage = 0;
-                ph ^= 1;
+                for (int kk = 0; kk < KSTEPS; ++kk)
+                  tc::mma2<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
+                                 (st > s0 || kk > 0) ? 1u : 0u);
+                tc::commit2_mc(&empty[stage], (uint16_t)0x3);
+                if (++stage == PSTAGES) {
+                  stage = 0;
+                  ph ^= 1;
+                }
               }
+              tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
+              acc_ph[buf] ^= 1;
+              buf ^= 1;
             }
-            tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
-            acc_ph[buf] ^= 1;
-            buf ^= 1;
           }
         }
       }
@@ -589,22 +595,24 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
-        const int total = (p.group_begin[g + 1] - p.group_begin[g]) * p.kblocks;
-        const int chunk = p.chunk_kb[g];
-        for (int s0 = 0; s0 < total; s0 += chunk) {
-          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-            report_status(p.status, DEV_TIMEOUT_MMA);
-            *abort_flag = 1;
-            goto epi_done;
+        for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
+          const int total = p.kblocks;
+          const int chunk = p.pair_chunk[pp];
+          for (int s0 = 0; s0 < total; s0 += chunk) {
+            if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+              report_status(p.status, DEV_TIMEOUT_MMA);
+              *abort_flag = 1;
+              goto epi_done;
+            }
+            tc::fence_after();
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+            drain_chunk<EPI, EPI_COLS>(taddr, S);
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
           }
-          tc::fence_after();
-          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-          drain_chunk<EPI, EPI_COLS>(taddr, S);
-          tc::fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
-          acc_ph[buf] ^= 1;
-          buf ^= 1;
         }
         if (EPI == EPI_OZAKI) {
           if (row < p.m) {
