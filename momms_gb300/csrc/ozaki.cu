@@ -660,20 +660,22 @@ constexpr int kMaxChunks = 8;
 // Column chunks of one emulated call: n cut at multiples of the tile width.
 // Calls whose B / C arrive from host memory take 4 chunks of at least 1024
 // columns (4096^3: e2e 5.40 -> 4.60 ms, 8192^3: 31.2 -> 28.3 ms; 6 or 8
-// chunks were no better); device-resident calls of at least 2^36 flops take
-// chunks of at least 2048 columns, which fill the products' tail with the
-// next chunk's preparation (4096^3: 3.53 -> 3.48 ms).
+// chunks were no better). Device-resident calls run unchunked: chunks there
+// only moved the next chunk's preparation into the products' tail (8192^3:
+// 20.65 vs 20.55 ms, 4096^3: 2.81 vs 2.77 ms), and one launch keeps the
+// slice kernel's own timing clean.
 // MOMMS_OZAKI_CHUNKS=1..8 fixes the count for A/B measurements; the results
 // are the same for every count (each entry's sums do not depend on it).
 int column_chunks(int64_t m, int64_t n, int64_t k, bool deferred) {
+  (void)m;
+  (void)k;
   const char* env = getenv("MOMMS_OZAKI_CHUNKS");
   if (env && *env) {
     const int v = atoi(env);
     if (v >= 1 && v <= kMaxChunks) return (int)std::min<int64_t>(v, ceil_div(n, sp::BN));
   }
   if (deferred) return (int)std::max<int64_t>(1, std::min<int64_t>(4, n / 1024));
-  if ((double)m * (double)n * (double)k < 6.0e10) return 1;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(4, n / 2048));
+  return 1;
 }
 }  // namespace
 
