@@ -658,9 +658,10 @@ namespace {
 constexpr int kMaxChunks = 8;
 
 // Column chunks of one emulated call: n cut at multiples of the tile width.
-// Calls whose B / C arrive from host memory take 4 chunks of at least 1024
-// columns (4096^3: e2e 5.40 -> 4.60 ms, 8192^3: 31.2 -> 28.3 ms; 6 or 8
-// chunks were no better). Device-resident calls run unchunked: chunks there
+// Calls whose B / C arrive from host memory take 5 chunks (column_cuts; 4
+// equal chunks took 4096^3 e2e from 5.40 to 4.60 ms and 8192^3 from 31.2 to
+// 28.3 ms with 7-bit digits; 6 or 8 equal chunks were no better).
+// Device-resident calls run unchunked: chunks there
 // only moved the next chunk's preparation into the products' tail (8192^3:
 // 20.65 vs 20.55 ms, 4096^3: 2.81 vs 2.77 ms), and one launch keeps the
 // slice kernel's own timing clean.
@@ -674,8 +675,21 @@ int column_chunks(int64_t m, int64_t n, int64_t k, bool deferred) {
     const int v = atoi(env);
     if (v >= 1 && v <= kMaxChunks) return (int)std::min<int64_t>(v, ceil_div(n, sp::BN));
   }
-  if (deferred) return (int)std::max<int64_t>(1, std::min<int64_t>(4, n / 1024));
+  if (deferred) return n >= 2048 ? 5 : (n >= 1024 ? 2 : 1);
   return 1;
+}
+
+// Chunk boundaries (multiples of the tile width, the last at n). Five chunks
+// of host-staged operands are cut 1/8, 1/4, 1/4, 1/4, 1/8: the first chunk's
+// B copy delays the first slice products, and the last chunk's copy-back
+// follows them, so both ends are narrow.
+void column_cuts(int64_t n, int nch, bool deferred, int64_t* cut) {
+  static const int kEighths[6] = {0, 1, 3, 5, 7, 8};
+  for (int c = 0; c < nch; ++c) {
+    const int64_t x = (deferred && nch == 5) ? n * kEighths[c] / 8 : n * c / nch;
+    cut[c] = std::min<int64_t>(n, round_up(x, sp::BN));
+  }
+  cut[nch] = n;
 }
 }  // namespace
 
@@ -746,8 +760,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const bool defer_b = stg && stg->deferred[1], defer_c = stg && stg->deferred[2];
   const int nch = (cap == cudaStreamCaptureStatusNone && ds->aux) ? column_chunks(m, n, k, defer_b || defer_c) : 1;
   int64_t cut[kMaxChunks + 1];
-  for (int c = 0; c < nch; ++c) cut[c] = std::min<int64_t>(n, round_up(n * c / nch, sp::BN));
-  cut[nch] = n;
+  column_cuts(n, nch, defer_b || defer_c, cut);
   const bool choose = ns_fixed == 0 && slices <= 0;
 
   // Deferred copies in the order they are read: B's sampled columns (the
