@@ -111,12 +111,12 @@ __global__ void __launch_bounds__(dmma::THREADS, 1)
   }
 }
 
+template <typename Off>
 __global__ void __launch_bounds__(ffma::THREADS, 2)
     sgemm_grouped_kernel(const SProblem* __restrict__ probs, int nprobs, int64_t total_units,
                          unsigned long long* next_unit, float* partials, unsigned* counters) {
   using namespace ffma;
-  __shared__ __align__(16) float As[2][BK][BM];
-  __shared__ __align__(16) float Bs[2][BK][BN];
+  extern __shared__ float4 ffma_smem[];
   __shared__ int s_last;
   __shared__ long long s_unit;
   for (;;) {
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(ffma::THREADS, 2)
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-    ffma_unit(P.o, tm, tn, kb0, kb1, acc, As, Bs);
+    ffma_unit_any<Off>(P.o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
     ffma_finish(P.e, acc, tm, tn, P.splits, sp,
                 P.splits > 1 ? partials + P.part_offset + (size_t)tile * P.splits * BM * BN : nullptr,
                 P.splits > 1 ? counters + P.counter_offset + tile : nullptr, &s_last);
@@ -188,6 +188,7 @@ struct Plan {
   float* s_partials = nullptr;
   unsigned* s_counters = nullptr;
   unsigned long long* s_next = nullptr;
+  bool s_wide = false;  // some f32 operand needs 64-bit element offsets
   // problems run by their own launch sequence (Ozaki, split-TF32)
   std::vector<PlanProblem> other;
   // operands copied to column-major scratch before each launch (f64
@@ -445,6 +446,7 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
                        a_ld % 4 == 0 && b_ld % 4 == 0;
       P.o = Operands{static_cast<const float*>(va.ptr), va.rs, va.cs, static_cast<const float*>(vb.ptr), vb.rs,
                      vb.cs, d.m, d.n, d.k, a_xc, b_xc, vec};
+      if (!offsets_fit_32(P.o)) p->s_wide = true;
       P.e = Epi{d.m, d.n, (float)d.alpha, (float)d.beta, static_cast<float*>(d.c.ptr), d.c.rs, d.c.cs};
       P.tiles_m = (int)ceil_div(d.m, BM);
       P.tiles_n = (int)ceil_div(d.n, BN);
@@ -536,8 +538,12 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     const int sms = (max_sms > 0 && max_sms < ds->sm_count) ? max_sms : ds->sm_count;
     const int grid = (int)std::min<int64_t>(p->s_units, 2 * sms);
     KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
-    grouped::sgemm_grouped_kernel<<<grid, ffma::THREADS, 0, s>>>(p->s_probs, p->ns, p->s_units, p->s_next,
-                                                                 p->s_partials, p->s_counters);
+    if (p->s_wide)
+      grouped::sgemm_grouped_kernel<uint64_t><<<grid, ffma::THREADS, ffma::SMEM_BYTES, s>>>(p->s_probs, p->ns, p->s_units,
+                                                                           p->s_next, p->s_partials, p->s_counters);
+    else
+      grouped::sgemm_grouped_kernel<uint32_t><<<grid, ffma::THREADS, ffma::SMEM_BYTES, s>>>(p->s_probs, p->ns, p->s_units,
+                                                                           p->s_next, p->s_partials, p->s_counters);
     note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
   }

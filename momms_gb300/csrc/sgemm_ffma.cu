@@ -3,7 +3,7 @@
 // The GPU form of the reference's f32 path (the bli_sgemm_haswell_asm_6x16
 // register block, ukernels/bli_gemm_haswell_asm_d6x8.c:77-640, under the same
 // Goto loops): a persistent 128 x 128 CTA tile, 256 threads each owning an
-// 8 x 8 register block, k streamed in blocks of 8 through double-buffered
+// 8 x 8 register block, k streamed in blocks of 16 through double-buffered
 // shared memory. Global loads are 128-bit and coalesced along whichever index
 // of the operand is contiguous; k-contiguous operands are transposed on their
 // way into shared memory so that every inner-loop read is a conflict-free
@@ -24,33 +24,34 @@ struct Params {
   unsigned* counters;
 };
 
-template <bool A_XC, bool B_XC, bool VEC>
-__global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const Params p) {
-  __shared__ __align__(16) float As[2][BK][BM];
-  __shared__ __align__(16) float Bs[2][BK][BN];
+// SPLIT: the launch splits k (p.sched.splits > 1); without it the unit loop
+// carries no split bookkeeping, which keeps the main loop within 128
+// registers (2 CTAs per SM) without spilling.
+template <bool A_XC, bool B_XC, typename Off, bool SPLIT>
+__global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const __grid_constant__ Params p) {
+  extern __shared__ float4 ffma_smem[];
   __shared__ int s_last;
-  Operands o = p.o;
-  o.a_xc = A_XC;  // compile-time layout for this instantiation
-  o.b_xc = B_XC;
-  o.vec = VEC;
+  const Operands& o = p.o;
   const int64_t units = p.sched.units();
-  const int64_t kblocks = ceil_div_dev(o.k, BK);
-  const int64_t kb_split = p.sched.k_per_split / BK;
   for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
     int tm, tn, sp;
     p.sched.decode(u, tm, tn, sp);
-    const int64_t kb0 = sp * kb_split;
-    const int64_t kb1 = min(kblocks, kb0 + kb_split);
+    const int64_t kblocks = ceil_div_dev(o.k, BK);
+    const int64_t kb0 = SPLIT ? sp * (p.sched.k_per_split / BK) : 0;
+    const int64_t kb1 = SPLIT ? min(kblocks, kb0 + p.sched.k_per_split / BK) : kblocks;
     float acc[8][8];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-    ffma_unit(o, tm, tn, kb0, kb1, acc, As, Bs);
-    const int64_t tile = u / p.sched.splits;
-    ffma_finish(p.e, acc, tm, tn, p.sched.splits, sp,
-                p.partials ? p.partials + (size_t)tile * p.sched.splits * BM * BN : nullptr,
-                p.counters ? p.counters + tile : nullptr, &s_last);
+    ffma_unit_t<A_XC, B_XC, Off>(o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
+    if (SPLIT) {
+      const int64_t tile = u / p.sched.splits;
+      ffma_finish(p.e, acc, tm, tn, p.sched.splits, sp, p.partials + (size_t)tile * p.sched.splits * BM * BN,
+                  p.counters + tile, &s_last);
+    } else {
+      ffma_finish(p.e, acc, tm, tn, 1, 0, nullptr, nullptr, &s_last);
+    }
   }
 }
 
@@ -117,19 +118,19 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   const int grid = (int)std::min<int64_t>(p.sched.units(), slots);
   {
     KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
-    if (a_xc && b_xc) {
-      if (vec) sgemm_kernel<true, true, true><<<grid, THREADS, 0, s>>>(p);
-      else sgemm_kernel<true, true, false><<<grid, THREADS, 0, s>>>(p);
-    } else if (a_xc) {
-      if (vec) sgemm_kernel<true, false, true><<<grid, THREADS, 0, s>>>(p);
-      else sgemm_kernel<true, false, false><<<grid, THREADS, 0, s>>>(p);
-    } else if (b_xc) {
-      if (vec) sgemm_kernel<false, true, true><<<grid, THREADS, 0, s>>>(p);
-      else sgemm_kernel<false, true, false><<<grid, THREADS, 0, s>>>(p);
-    } else {
-      if (vec) sgemm_kernel<false, false, true><<<grid, THREADS, 0, s>>>(p);
-      else sgemm_kernel<false, false, false><<<grid, THREADS, 0, s>>>(p);
-    }
+    // one instantiation per (A layout, B layout, offset width, split)
+    typedef void (*Kern)(const Params);
+    static const Kern table[2][2][2][2] = {
+        {{{sgemm_kernel<false, false, uint32_t, false>, sgemm_kernel<false, false, uint32_t, true>},
+          {sgemm_kernel<false, false, uint64_t, false>, sgemm_kernel<false, false, uint64_t, true>}},
+         {{sgemm_kernel<false, true, uint32_t, false>, sgemm_kernel<false, true, uint32_t, true>},
+          {sgemm_kernel<false, true, uint64_t, false>, sgemm_kernel<false, true, uint64_t, true>}}},
+        {{{sgemm_kernel<true, false, uint32_t, false>, sgemm_kernel<true, false, uint32_t, true>},
+          {sgemm_kernel<true, false, uint64_t, false>, sgemm_kernel<true, false, uint64_t, true>}},
+         {{sgemm_kernel<true, true, uint32_t, false>, sgemm_kernel<true, true, uint32_t, true>},
+          {sgemm_kernel<true, true, uint64_t, false>, sgemm_kernel<true, true, uint64_t, true>}}}};
+    const Kern k = table[a_xc][b_xc][offsets_fit_32(p.o) ? 0 : 1][splits > 1 ? 1 : 0];
+    k<<<grid, THREADS, SMEM_BYTES, s>>>(p);
   }
   note_launch();
   ce = cudaGetLastError();

@@ -7,7 +7,7 @@
 // The split-k count comes from a measured table filled by momms_autotune()
 // (candidates timed with CUDA events on scratch output) or, for shapes not in
 // the table, from a model: split k only when the output tiles cannot fill the
-// GPU, keeping at least 4 (f64) / 16 (f32) k-blocks per split.
+// GPU, keeping at least 4 (f64, 64 of k) / 8 (f32, 128 of k) k-blocks per split.
 #include <stdio.h>
 #include <string.h>
 
@@ -58,9 +58,9 @@ int splits_f64(int64_t m, int64_t n, int64_t k, int sm_count) {
 }
 
 int splits_f32(int64_t m, int64_t n, int64_t k, int sm_count) {
-  const int64_t tiles = ceil_div(m, 128) * ceil_div(n, 128), kblocks = ceil_div(k, 8);
+  const int64_t tiles = ceil_div(m, 128) * ceil_div(n, 128), kblocks = ceil_div(k, 16);
   int s = lookup(MOMMS_DTYPE_F32, MOMMS_PREC_PLAIN, m, n, k);
-  if (s <= 0) s = model_splits(tiles, kblocks, 2 * sm_count, 16);
+  if (s <= 0) s = model_splits(tiles, kblocks, 2 * sm_count, 8);
   return std::max(1, (int)std::min<int64_t>(s, std::max<int64_t>(1, kblocks)));
 }
 
@@ -80,7 +80,7 @@ int momms_autotune(const momms_gemm_desc* desc, momms_tune_result* out, void* st
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t es = desc->dtype == MOMMS_DTYPE_F64 ? 8 : 4;
-  const int bk = desc->dtype == MOMMS_DTYPE_F64 ? 16 : 8;
+  const int bk = 16;  // k-block of both the DMMA and the FFMA kernels
   const int64_t kblocks = ceil_div(desc->k, bk);
   // scratch C so that the caller's C is not touched
   void* cs = nullptr;
