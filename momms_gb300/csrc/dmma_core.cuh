@@ -155,21 +155,58 @@ __device__ __forceinline__ bool consume_unit(bool a_xc, bool b_xc, int64_t kb0, 
 // `counter` sums all partials in split order 0..splits-1 (a fixed order: the
 // result does not depend on which CTA finishes last), writes C and resets
 // the counter to zero.
+//
+// A thread's 64 outputs are handled in groups of EPI_ROWS 8-row blocks (8
+// outputs each): every load of a group (C for beta != 0, the partials of one
+// split) is issued before the first value is used, so a group costs one
+// memory round trip per pass instead of one per element.
+constexpr int EPI_ROWS = 1;
 __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2], int64_t row0, int64_t col0,
                                             int splits, int sp, double* tile_partials, unsigned* counter, int ctid,
                                             int* s_last) {
-  if (splits == 1) {
+  constexpr int G = EPI_ROWS;
+  const size_t tile_elems = (size_t)BM * BN;
+  // element (i, j, q) of this thread: row row0 + 8i, column col0 + 8j + q
+  auto live = [&](int i, int j, int q) { return row0 + i * 8 < e.m && col0 + j * 8 + q < e.n; };
+  auto cptr = [&](int i, int j, int q) { return e.c + (row0 + i * 8) * e.rsc + (col0 + j * 8 + q) * e.csc; };
+  auto slot = [&](int i, int j, int q) { return ((i * 4 + j) * 2 + q) * CONSUMERS + ctid; };
+  // C = beta*C + alpha*v for block rows g*G .. g*G+G-1
+  auto update_group = [&](int g, const double (&v)[G][4][2]) {
+    double c0[G][4][2];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int ii = 0; ii < G; ++ii)
 #pragma unroll
       for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int q = 0; q < 2; ++q) store_c(e, row0 + i * 8, col0 + j * 8 + q, acc[i][j][q]);
+        for (int q = 0; q < 2; ++q)
+          c0[ii][j][q] = (e.beta != 0.0 && live(g * G + ii, j, q)) ? *cptr(g * G + ii, j, q) : 0.0;
+#pragma unroll
+    for (int ii = 0; ii < G; ++ii)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+          if (live(g * G + ii, j, q)) {
+            const double t = v[ii][j][q] * e.alpha;
+            *cptr(g * G + ii, j, q) = (e.beta == 0.0) ? t : fma(e.beta, c0[ii][j][q], t);
+          }
+  };
+  if (splits == 1) {
+#pragma unroll
+    for (int g = 0; g < 8 / G; ++g) {
+      double v[G][4][2];
+#pragma unroll
+      for (int ii = 0; ii < G; ++ii)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int q = 0; q < 2; ++q) v[ii][j][q] = acc[g * G + ii][j][q];
+      update_group(g, v);
+    }
     return;
   }
   // Partials exist only for the tile's entries inside C: a small problem's
   // mostly-empty tile writes and re-reads just its live part.
-  const size_t tile_elems = (size_t)BM * BN;
   double* part = tile_partials + (size_t)sp * tile_elems;
 #pragma unroll
   for (int i = 0; i < 8; ++i)
@@ -177,7 +214,7 @@ __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2]
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int q = 0; q < 2; ++q)
-        if (row0 + i * 8 < e.m && col0 + j * 8 + q < e.n) part[((i * 4 + j) * 2 + q) * CONSUMERS + ctid] = acc[i][j][q];
+        if (live(i, j, q)) part[slot(i, j, q)] = acc[i][j][q];
   __threadfence();
   consumer_sync();
   if (ctid == 0) {
@@ -188,17 +225,33 @@ __device__ __forceinline__ void finish_unit(const Epi& e, double (&acc)[8][4][2]
   if (*s_last) {
     __threadfence();
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int g = 0; g < 8 / G; ++g) {
+      double v[G][4][2];
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int ii = 0; ii < G; ++ii)
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          if (row0 + i * 8 >= e.m || col0 + j * 8 + q >= e.n) continue;
-          const int r = ((i * 4 + j) * 2 + q) * CONSUMERS + ctid;
-          double s = __ldcg(tile_partials + r);
-          for (int t = 1; t < splits; ++t) s += __ldcg(tile_partials + (size_t)t * tile_elems + r);
-          store_c(e, row0 + i * 8, col0 + j * 8 + q, s);
-        }
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+            v[ii][j][q] = live(g * G + ii, j, q) ? __ldcg(tile_partials + slot(g * G + ii, j, q)) : 0.0;
+      for (int t = 1; t < splits; ++t) {
+        const double* pt = tile_partials + (size_t)t * tile_elems;
+        double w[G][4][2];
+#pragma unroll
+        for (int ii = 0; ii < G; ++ii)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) w[ii][j][q] = live(g * G + ii, j, q) ? __ldcg(pt + slot(g * G + ii, j, q)) : 0.0;
+#pragma unroll
+        for (int ii = 0; ii < G; ++ii)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) v[ii][j][q] += w[ii][j][q];
+      }
+      update_group(g, v);
+    }
     if (ctid == 0) *counter = 0u;
   }
   consumer_sync();
