@@ -4,8 +4,8 @@
 //
 // Every plain f64 problem contributes tiles x splits work units to one
 // persistent DMMA kernel and every plain f32 problem to one persistent FFMA
-// kernel. Units are ordered by decreasing cost (longest first) and dealt to
-// the CTAs round-robin (f64) or through a global atomic counter (f32). The
+// kernel. Units are ordered by decreasing cost (longest first) and handed to
+// the CTAs through a global atomic counter. The
 // split count of each problem is chosen so that no unit is much larger than
 // the batch's average share per SM (the runtime analogue of the reference's
 // compile-time block sizes); its k-splits are reduced in a fixed order, so a
@@ -57,57 +57,111 @@ __device__ __forceinline__ int find_problem(const P* probs, int nprobs, int64_t 
   return lo;
 }
 
+// Decodes unit u of the f64 group: its problem, output tile and k-blocks.
+struct DUnit {
+  int pi, tm, tn, sp;
+  int64_t tile, kb0, kb1;
+};
+__device__ __forceinline__ DUnit decode_dunit(const DProblem* probs, int nprobs, int64_t u) {
+  using namespace dmma;
+  DUnit d;
+  d.pi = find_problem(probs, nprobs, u);
+  const DProblem& P = probs[d.pi];
+  const int64_t local = u - P.unit_begin;
+  d.sp = (int)(local % P.splits);
+  d.tile = local / P.splits;
+  d.tm = (int)(d.tile % P.tiles_m);
+  d.tn = (int)(d.tile / P.tiles_m);
+  const int64_t kblocks = ceil_div_dev(P.k, BK);
+  d.kb0 = d.sp * P.kb_split;
+  d.kb1 = min(kblocks, d.kb0 + P.kb_split);
+  return d;
+}
+
+// Units are handed out dynamically: the producer lane takes the next unit
+// from a global counter (units are numbered largest problem first, so this
+// is longest-processing-time-first list scheduling, balanced by the actual
+// unit durations rather than a cost model) and tags the first pipeline stage
+// it fills for that unit with the unit's index; the DMMA warps read the tag
+// when they reach that stage. An index of -1 ends the kernel. The last CTA
+// to finish resets the counter, so a captured plan relaunches as is.
 __global__ void __launch_bounds__(dmma::THREADS, 1)
     dgemm_grouped_kernel(const CUtensorMap* __restrict__ maps, const DProblem* __restrict__ probs, int nprobs,
-                         int64_t total_units, double* partials, unsigned* counters, unsigned* status) {
+                         int64_t total_units, double* partials, unsigned* counters, unsigned long long* next_unit,
+                         unsigned* status) {
   using namespace dmma;
   extern __shared__ uint8_t smem_raw[];
+  __shared__ long long s_stage_unit[STAGES];  // unit starting at each stage, -1: end
   const Smem sm = setup_smem(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int stage = 0;
   uint32_t phase = 0;
   if (warp == CONSUMER_WARPS) {
     if (lane == 0) {
-      for (int64_t u = blockIdx.x; u < total_units; u += gridDim.x) {
-        const int pi = find_problem(probs, nprobs, u);
-        const DProblem& P = probs[pi];
-        const int64_t local = u - P.unit_begin;
-        const int sp = (int)(local % P.splits);
-        const int64_t tile = local / P.splits;
-        const int tm = (int)(tile % P.tiles_m), tn = (int)(tile / P.tiles_m);
-        const int64_t kblocks = ceil_div_dev(P.k, BK);
-        const int64_t kb0 = sp * P.kb_split, kb1 = min(kblocks, kb0 + P.kb_split);
-        if (!produce_unit(&maps[2 * pi], &maps[2 * pi + 1], P.flags & 1, (P.flags >> 1) & 1, tm, tn, kb0, kb1, sm.sA,
-                          sm.sB, sm.full, sm.empty, stage, phase, status))
-          return;
+      bool ok = true;
+      for (;;) {
+        const long long u = (long long)atomicAdd(next_unit, 1ull);
+        if (u >= total_units) break;
+        const DUnit d = decode_dunit(probs, nprobs, u);
+        const DProblem& P = probs[d.pi];
+        // the tag is written while the stage is free (every DMMA warp read
+        // the previous tag before releasing it) and published by the
+        // stage's arrive (release) to the warps' wait (acquire)
+        if (!mbar_wait_bounded(&sm.empty[stage], phase ^ 1)) {
+          report_status(status, DEV_TIMEOUT_EMPTY);
+          ok = false;
+          break;
+        }
+        s_stage_unit[stage] = u;
+        if (!produce_unit(&maps[2 * d.pi], &maps[2 * d.pi + 1], P.flags & 1, (P.flags >> 1) & 1, d.tm, d.tn, d.kb0,
+                          d.kb1, sm.sA, sm.sB, sm.full, sm.empty, stage, phase, status)) {
+          ok = false;
+          break;
+        }
+      }
+      if (ok) {
+        if (mbar_wait_bounded(&sm.empty[stage], phase ^ 1)) {
+          s_stage_unit[stage] = -1;
+          mbar_arrive(&sm.full[stage]);
+        } else {
+          report_status(status, DEV_TIMEOUT_EMPTY);
+        }
+      }
+      // the last CTA out resets the unit counter for the next launch
+      __threadfence();
+      const unsigned long long done = atomicAdd(next_unit + 1, 1ull);
+      if (done == (unsigned long long)gridDim.x - 1) {
+        next_unit[0] = 0ull;
+        next_unit[1] = 0ull;
+        __threadfence();
       }
     }
     return;
   }
   const int wm = warp >> 2, wn = warp & 3;
-  for (int64_t u = blockIdx.x; u < total_units; u += gridDim.x) {
-    const int pi = find_problem(probs, nprobs, u);
-    const DProblem& P = probs[pi];
-    const int64_t local = u - P.unit_begin;
-    const int sp = (int)(local % P.splits);
-    const int64_t tile = local / P.splits;
-    const int tm = (int)(tile % P.tiles_m), tn = (int)(tile / P.tiles_m);
-    const int64_t kblocks = ceil_div_dev(P.k, BK);
-    const int64_t kb0 = sp * P.kb_split, kb1 = min(kblocks, kb0 + P.kb_split);
-    const int64_t row_base = (int64_t)tm * BM + wm * 64, col_base = (int64_t)tn * BN + wn * 32;
+  for (;;) {
+    if (!mbar_wait_bounded(&sm.full[stage], phase)) {
+      report_status(status, DEV_TIMEOUT_FULL);
+      return;
+    }
+    const long long u = s_stage_unit[stage];
+    if (u < 0) break;
+    const DUnit d = decode_dunit(probs, nprobs, u);
+    const DProblem& P = probs[d.pi];
+    const int64_t row_base = (int64_t)d.tm * BM + wm * 64, col_base = (int64_t)d.tn * BN + wn * 32;
     const uint32_t live = live_mask(row_base, col_base, P.m, P.n);
     double acc[8][4][2];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-    if (!consume_unit(P.flags & 1, (P.flags >> 1) & 1, kb0, kb1, live, sm.sA, sm.sB, sm.full, sm.empty, stage, phase,
-                      wm, wn, lane, acc, status))
+    if (!consume_unit(P.flags & 1, (P.flags >> 1) & 1, d.kb0, d.kb1, live, sm.sA, sm.sB, sm.full, sm.empty, stage,
+                      phase, wm, wn, lane, acc, status))
       return;
     const Epi e{P.m, P.n, P.alpha, P.beta, P.c, P.rsc, P.csc};
-    finish_unit(e, acc, row_base + (lane >> 2), col_base + 2 * (lane & 3), P.splits, sp,
-                P.splits > 1 ? partials + P.part_offset + (size_t)tile * P.splits * BM * BN : nullptr,
-                P.splits > 1 ? counters + P.counter_offset + tile : nullptr, threadIdx.x, sm.s_last);
+    finish_unit(e, acc, row_base + (lane >> 2), col_base + 2 * (lane & 3), P.splits, d.sp,
+                P.splits > 1 ? partials + P.part_offset + (size_t)d.tile * P.splits * BM * BN : nullptr,
+                P.splits > 1 ? counters + P.counter_offset + d.tile : nullptr, threadIdx.x, sm.s_last);
   }
 }
 
@@ -181,6 +235,7 @@ struct Plan {
   CUtensorMap* d_maps = nullptr;         // device
   double* d_partials = nullptr;
   unsigned* d_counters = nullptr;
+  unsigned long long* d_next = nullptr;  // unit counter + finished-CTA counter
   // f32 plain group
   int ns = 0;
   int64_t s_units = 0;
@@ -412,7 +467,8 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
     if (!rc) { p->d_probs = static_cast<grouped::DProblem*>(buf); rc = plan_alloc(p, &buf, maps.size() * sizeof(CUtensorMap)); }
     if (!rc) { p->d_maps = static_cast<CUtensorMap*>(buf); rc = plan_alloc(p, &buf, (size_t)parts * 8); }
     if (!rc) { p->d_partials = static_cast<double*>(buf); rc = plan_alloc(p, &buf, (size_t)ctrs * 4); }
-    if (!rc) p->d_counters = static_cast<unsigned*>(buf);
+    if (!rc) { p->d_counters = static_cast<unsigned*>(buf); rc = plan_alloc(p, &buf, 2 * sizeof(unsigned long long)); }
+    if (!rc) p->d_next = static_cast<unsigned long long*>(buf);
     if (rc) { plan_free(p); return rc; }
     size_t off = p->host_tables.size();
     rc = plan_upload(p, p->d_probs, probs.data(), probs.size() * sizeof(grouped::DProblem));
@@ -421,6 +477,7 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
     if (!rc) rc = plan_upload(p, p->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap));
     if (!rc && async) pending.push_back({p->d_maps, {off, maps.size() * sizeof(CUtensorMap)}});
     if (!rc) rc = plan_zero(p, p->d_counters, (size_t)ctrs * 4);
+    if (!rc) rc = plan_zero(p, p->d_next, 2 * sizeof(unsigned long long));
     if (rc) { plan_free(p); return rc; }
   }
 
@@ -530,7 +587,7 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     const int grid = (int)std::min<int64_t>(p->d_units, sms);
     KernelTimer kt(MOMMS_KERNEL_DGEMM_DMMA, s);
     grouped::dgemm_grouped_kernel<<<grid, dmma::THREADS, dmma::SMEM_BYTES, s>>>(
-        p->d_maps, p->d_probs, p->nd, p->d_units, p->d_partials, p->d_counters, ds->status);
+        p->d_maps, p->d_probs, p->nd, p->d_units, p->d_partials, p->d_counters, p->d_next, ds->status);
     note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f64 launch");
   }
