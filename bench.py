@@ -103,9 +103,14 @@ def max_over_ranks(x, world):
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
+    """nvidia-smi sampling every 50 ms, started before the warm-up (the tool
+    takes a moment to start); each line is stamped on arrival and stop()
+    keeps the samples that arrived inside the timed window [t0, t1] (plus one
+    interval, a sample describing the moment before it is printed)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, device):
         self.device = device
@@ -116,7 +121,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.PERIOD_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
         except (OSError, FileNotFoundError):
@@ -124,9 +129,9 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -136,7 +141,15 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if t0 is not None and t1 is not None:
+            inside = [ln for t, ln in lines if t0 <= t <= t1 + self.PERIOD_MS * 1e-3]
+            # a window shorter than the period: the first sample after it starts
+            after = [ln for t, ln in lines if t >= t0][:1]
+            lines = inside or after
+        else:
+            lines = [ln for _, ln in lines]
+        for ln in lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -543,18 +556,19 @@ def run_ours(args):
         _kernel_ms(lib, mg, cls)  # reset
 
     # ---- emulated FP64: the timed region of the headline value ----
+    clocks = ClockSampler(local)
+    clocks.start()
     _timed_steps(lib, mg, torch, stream, emu_desc, dC, dC0, 0, args.warmup)
     for cls in range(6):
         _kernel_ms(lib, mg, cls)  # reset: count the timed steps only
-    clocks = ClockSampler(local)
-    clocks.start()
     barrier(world)
     torch.cuda.synchronize()
     t_start = time.perf_counter()
     step_ms, launches = _timed_steps(lib, mg, torch, stream, emu_desc, dC, dC0, args.steps, 0)
     torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_start
-    clk = clocks.stop()
+    t_end = time.perf_counter()
+    t_wall = t_end - t_start
+    clk = clocks.stop(t_start, t_end)
     info = mg.CallInfo()
     lib.momms_last_info(ctypes.byref(info))
     slice_ms, slice_n = _kernel_ms(lib, mg, mg.KERNEL_SLICE_OZAKI)
