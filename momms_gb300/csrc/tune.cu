@@ -7,7 +7,7 @@
 // The split-k count comes from a measured table filled by momms_autotune()
 // (candidates timed with CUDA events on scratch output) or, for shapes not in
 // the table, from a model: split k only when the output tiles cannot fill the
-// GPU, keeping at least 4 (f64, 64 of k) / 8 (f32, 128 of k) k-blocks per split.
+// GPU, keeping at least 2 (f64, 32 of k) / 8 (f32, 128 of k) k-blocks per split.
 #include <stdio.h>
 #include <string.h>
 
@@ -49,11 +49,13 @@ int splits_f64(int64_t m, int64_t n, int64_t k, int sm_count) {
   const int64_t tiles = ceil_div(m, 128) * ceil_div(n, 128), kblocks = ceil_div(k, 16);
   int s = lookup(MOMMS_DTYPE_F64, MOMMS_PREC_PLAIN, m, n, k);
   // Small problems: one SM's FP64 rate is ~7 GFLOP/s, so splitting k down to
-  // four k-blocks (64) per unit beats leaving SMs idle (256^3: 0.61 -> 0.33
-  // ms). Two k-blocks made 256^3 faster still (0.21 ms) but a batch of 512
-  // small problems 25 % slower in the grouped kernel, where the splits' fixed
-  // costs (pipeline fill, partial write, reduction) buy no parallelism.
-  if (s <= 0) s = model_splits(tiles, kblocks, sm_count, 4);
+  // two k-blocks (32) per unit beats leaving SMs idle. Measured on GB300 with
+  // the dynamically scheduled grouped kernel: 256^3 0.33 -> 0.21 ms and 128^3
+  // 0.32 -> 0.19 ms against four k-blocks per unit, while a batch of 239 small
+  // f64 problems, whose splits' fixed costs (pipeline fill, partial write,
+  // reduction) buy no parallelism, took 3 % longer (14.2 -> 14.7 ms); one
+  // k-block per unit gained 256^3 another 20 % but cost the batch 8 %.
+  if (s <= 0) s = model_splits(tiles, kblocks, sm_count, 2);
   return std::max(1, (int)std::min<int64_t>(s, std::max<int64_t>(1, kblocks)));
 }
 
