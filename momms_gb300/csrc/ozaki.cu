@@ -604,13 +604,18 @@ namespace {
 // (t, d-t) in t order, cut into accumulation groups whose worst-case int32
 // sums (k * 2^bits_t * 2^bits_u over the group's pairs; the top digit has
 // `bits` bits, the centred ones bits-1) stay within kGroupLimit. A group's
-// Each pair's TMEM chunks keep one chunk's sum within kChunkBound for that
-// pair's largest digit product (4, 8 or 16 k-blocks of 64 for 8-bit digits).
+// A TMEM chunk keeps its sum within kChunkBound: a k-block of pair (t, u)
+// adds at most 64 * 2^bits_t * 2^bits_u, so a pair's weight is that product
+// in units of 2^10 and a chunk's capacity kChunkBound / 64 / 2^10 (a lone
+// pair: 4, 8 or 16 k-blocks of 64 for 8-bit digits; at small k one chunk
+// spans several pairs of a group).
+constexpr int kChunkUnitLog2 = 10;
+constexpr int kChunkCap = (int)(kChunkBound / 64.0) >> kChunkUnitLog2;
 struct Schedule {
   int np = 0, ng = 0;
   uint8_t pair_a[sp::MAX_PAIRS], pair_b[sp::MAX_PAIRS];
   int group_begin[sp::MAX_GROUPS + 1];
-  int pair_chunk[sp::MAX_PAIRS];
+  int pair_w[sp::MAX_PAIRS];
   uint8_t level[sp::MAX_GROUPS];  // d - 2
 };
 
@@ -639,7 +644,7 @@ bool ozaki_schedule(int ns, int64_t k, Schedule* sc) {
       if (sc->np >= sp::MAX_PAIRS) return false;
       sc->pair_a[sc->np] = (uint8_t)(t - 1);
       sc->pair_b[sc->np] = (uint8_t)(u - 1);
-      sc->pair_chunk[sc->np] = (int)std::max<int64_t>(1, (int64_t)(kChunkBound / pb) / 64);
+      sc->pair_w[sc->np] = std::max(1, (int)ldexp(pb, -kChunkUnitLog2));
       ++sc->np;
       gsum += kspan * pb;
     }
@@ -856,7 +861,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   memcpy(p.pair_a, sch.pair_a, (size_t)np);
   memcpy(p.pair_b, sch.pair_b, (size_t)np);
   memcpy(p.group_begin, sch.group_begin, sizeof(int) * (size_t)(ng + 1));
-  memcpy(p.pair_chunk, sch.pair_chunk, sizeof(int) * (size_t)np);
+  memcpy(p.pair_w, sch.pair_w, sizeof(int) * (size_t)np);
+  p.chunk_cap = kChunkCap;
+  p.merge_pairs = 1;
   p.ngroups = ng;
   call_info().slices = ns;
   call_info().pairs = np;

@@ -105,7 +105,11 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   p.pair_a[0] = 1; p.pair_b[0] = 0;  // A_lo * B_hi
   p.pair_a[1] = 0; p.pair_b[1] = 1;  // A_hi * B_lo
   p.pair_a[2] = 0; p.pair_b[2] = 0;  // A_hi * B_hi
-  for (int i = 0; i < 3; ++i) p.pair_chunk[i] = 8;  // 256 k per tensor-core accumulation, then an RN add in registers
+  // 256 k per tensor-core accumulation (8 k-blocks of one pair), then an RN
+  // add in registers; chunks never span pairs
+  for (int i = 0; i < 3; ++i) p.pair_w[i] = 1;
+  p.chunk_cap = 8;
+  p.merge_pairs = 0;
   p.alpha_f = (float)g.alpha;
   p.beta_f = (float)g.beta;
   p.c32 = static_cast<float*>(g.c.ptr);

@@ -4,8 +4,9 @@
 //   for each output tile (persistent, one CTA per SM, 128 x 256 tiles):
 //     for each group g (processed in order):
 //       S_g = sum over pairs (a, b) in g of  A_plane[a] * B_plane[b]^T
-//       accumulated in TMEM, each pair in chunks of pair_chunk k-blocks; each
-//       finished chunk is handed to the epilogue (ping-pong TMEM buffers)
+//       accumulated in TMEM in chunks (runs of (pair, k-block) steps within a
+//       bound, Params::pair_w); each finished chunk is handed to the
+//       epilogue (ping-pong TMEM buffers)
 //
 // Planes are K-major in HBM ([plane][row][k], k contiguous) and are loaded by
 // TMA as 128-byte-wide k-blocks with the 128B swizzle that the tcgen05 shared
@@ -73,7 +74,15 @@ struct Params {
   int ngroups;
   int gchunk;  // groups per work unit: a tile's groups may run as separate units (0 = all)
   int group_begin[MAX_GROUPS + 1];
-  int pair_chunk[MAX_PAIRS];  // k-blocks per TMEM accumulation chunk of each pair
+  // TMEM accumulation chunks: a chunk is a run of consecutive (pair, k-block)
+  // steps of one group whose weights pair_w sum to at most chunk_cap; with
+  // merge_pairs a chunk continues from one pair into the next (the Ozaki
+  // path, whose chunk sums are exact, so chunking never changes a result),
+  // otherwise every pair starts a new chunk. group_chunks[g]: chunks of
+  // group g (plan_chunks).
+  int pair_w[MAX_PAIRS];
+  int chunk_cap, merge_pairs;
+  int group_chunks[MAX_GROUPS];
   uint8_t pair_a[MAX_PAIRS], pair_b[MAX_PAIRS];
   // EPI_F32
   float alpha_f, beta_f;
@@ -262,19 +271,39 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t t = unit_at(r);
         if (t >= units) continue;
         for (int g = g_begin(t); g < g_end(t); ++g) {
+          int load = 0;
+          bool open = false;
+          uint32_t d_tmem = 0;
           for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-            const int total = p.kblocks;
-            const int chunk = p.pair_chunk[pp];
-            for (int s0 = 0; s0 < total; s0 += chunk) {
-              if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-                report_status(p.status, DEV_TIMEOUT_TMEM);
-                *abort_flag = 1;
-                goto mma_done;
+            const int w = p.pair_w[pp];
+            if (open && !p.merge_pairs) {
+              tc::commit(&tfull[buf]);
+              acc_ph[buf] ^= 1;
+              buf ^= 1;
+              open = false;
+            }
+            for (int st = 0; st < p.kblocks;) {
+              if (open && load + w > p.chunk_cap) {
+                tc::commit(&tfull[buf]);
+                acc_ph[buf] ^= 1;
+                buf ^= 1;
+                open = false;
               }
-              tc::fence_after();
-              const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-              const int s1 = min(total, s0 + chunk);
-              for (int st = s0; st < s1; ++st) {
+              bool fresh = false;
+              if (!open) {
+                if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+                  report_status(p.status, DEV_TIMEOUT_TMEM);
+                  *abort_flag = 1;
+                  goto mma_done;
+                }
+                tc::fence_after();
+                d_tmem = tmem_base + (uint32_t)(buf * BN);
+                load = 0;
+                open = fresh = true;
+              }
+              // the k-blocks of this pair that still fit in the open chunk
+              const int s0 = st, s1 = min(p.kblocks, st + (p.chunk_cap - load) / w);
+              for (; st < s1; ++st) {
                 if (!mbar_wait_bounded(&full[stage], ph)) {
                   report_status(p.status, DEV_TIMEOUT_FULL);
                   *abort_flag = 1;
@@ -286,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int kk = 0; kk < KSTEPS; ++kk)
                   tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
-                                (st > s0 || kk > 0) ? 1u : 0u);
+                                (fresh && st == s0 && kk == 0) ? 0u : 1u);
                 if (MC)
                   tc::commit_mc(&empty[stage], (uint16_t)0x3);  // both CTAs' copies of the stage are free
                 else
@@ -296,10 +325,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                   ph ^= 1;
                 }
               }
-              tc::commit(&tfull[buf]);
-              acc_ph[buf] ^= 1;
-              buf ^= 1;
+              load += (s1 - s0) * w;
             }
+          }
+          if (open) {
+            tc::commit(&tfull[buf]);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
           }
         }
       }
@@ -332,24 +364,20 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
-        for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-          const int total = p.kblocks;
-          const int chunk = p.pair_chunk[pp];
-          for (int s0 = 0; s0 < total; s0 += chunk) {
-            if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-              report_status(p.status, DEV_TIMEOUT_MMA);
-              *abort_flag = 1;
-              goto epi_done;
-            }
-            tc::fence_after();
-            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-            drain_chunk<EPI, EPI_COLS>(taddr, S);
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[buf]);
-            acc_ph[buf] ^= 1;
-            buf ^= 1;
+        for (int c = 0; c < p.group_chunks[g]; ++c) {
+          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+            report_status(p.status, DEV_TIMEOUT_MMA);
+            *abort_flag = 1;
+            goto epi_done;
           }
+          tc::fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+          drain_chunk<EPI, EPI_COLS>(taddr, S);
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[buf]);
+          acc_ph[buf] ^= 1;
+          buf ^= 1;
         }
         if (EPI == EPI_OZAKI) {
           // end of group g: publish the exact int32 sums (column-major plane g)
@@ -366,14 +394,24 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
       if (EPI == EPI_F32 && row < p.m) {
+        // C is read 8 columns at a time, every load of a group issued before
+        // the first use (one memory round trip per group, not per element)
         float* crow = p.c32 + row * p.rsc;
 #pragma unroll
-        for (int j = 0; j < EPI_COLS; ++j) {
-          const int64_t col = col0 + j;
-          if (col < p.n) {
-            float* cp = crow + col * p.csc;
-            const float v = (float)S[j] * p.alpha_f;
-            *cp = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, *cp, v);
+        for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
+          float c0[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t col = col0 + j0 + j;
+            c0[j] = (p.beta_f != 0.0f && col < p.n) ? crow[col * p.csc] : 0.0f;
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t col = col0 + j0 + j;
+            if (col < p.n) {
+              const float v = (float)S[j0 + j] * p.alpha_f;
+              crow[col * p.csc] = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, c0[j], v);
+            }
           }
         }
       }
@@ -532,19 +570,39 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t t = unit_at(r);
         if (t >= units) continue;
         for (int g = g_begin(t); g < g_end(t); ++g) {
+          int load = 0;
+          bool open = false;
+          uint32_t d_tmem = 0;
           for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-            const int total = p.kblocks;
-            const int chunk = p.pair_chunk[pp];
-            for (int s0 = 0; s0 < total; s0 += chunk) {
-              if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-                report_status(p.status, DEV_TIMEOUT_TMEM);
-                *abort_flag = 1;
-                goto mma_done;
+            const int w = p.pair_w[pp];
+            if (open && !p.merge_pairs) {
+              tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
+              acc_ph[buf] ^= 1;
+              buf ^= 1;
+              open = false;
+            }
+            for (int st = 0; st < p.kblocks;) {
+              if (open && load + w > p.chunk_cap) {
+                tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
+                acc_ph[buf] ^= 1;
+                buf ^= 1;
+                open = false;
               }
-              tc::fence_after();
-              const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-              const int s1 = min(total, s0 + chunk);
-              for (int st = s0; st < s1; ++st) {
+              bool fresh = false;
+              if (!open) {
+                if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
+                  report_status(p.status, DEV_TIMEOUT_TMEM);
+                  *abort_flag = 1;
+                  goto mma_done;
+                }
+                tc::fence_after();
+                d_tmem = tmem_base + (uint32_t)(buf * BN);
+                load = 0;
+                open = fresh = true;
+              }
+              // the k-blocks of this pair that still fit in the open chunk
+              const int s0 = st, s1 = min(p.kblocks, st + (p.chunk_cap - load) / w);
+              for (; st < s1; ++st) {
                 if (!mbar_wait_bounded(&full[stage], ph)) {
                   report_status(p.status, DEV_TIMEOUT_FULL);
                   *abort_flag = 1;
@@ -556,17 +614,20 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int kk = 0; kk < KSTEPS; ++kk)
                   tc::mma2<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
-                                 (st > s0 || kk > 0) ? 1u : 0u);
+                                (fresh && st == s0 && kk == 0) ? 0u : 1u);
                 tc::commit2_mc(&empty[stage], (uint16_t)0x3);
                 if (++stage == PSTAGES) {
                   stage = 0;
                   ph ^= 1;
                 }
               }
-              tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
-              acc_ph[buf] ^= 1;
-              buf ^= 1;
+              load += (s1 - s0) * w;
             }
+          }
+          if (open) {
+            tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
+            acc_ph[buf] ^= 1;
+            buf ^= 1;
           }
         }
       }
@@ -595,24 +656,20 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
       for (int g = g_begin(t); g < g_end(t); ++g) {
-        for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-          const int total = p.kblocks;
-          const int chunk = p.pair_chunk[pp];
-          for (int s0 = 0; s0 < total; s0 += chunk) {
-            if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-              report_status(p.status, DEV_TIMEOUT_MMA);
-              *abort_flag = 1;
-              goto epi_done;
-            }
-            tc::fence_after();
-            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
-            drain_chunk<EPI, EPI_COLS>(taddr, S);
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
-            acc_ph[buf] ^= 1;
-            buf ^= 1;
+        for (int c = 0; c < p.group_chunks[g]; ++c) {
+          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
+            report_status(p.status, DEV_TIMEOUT_MMA);
+            *abort_flag = 1;
+            goto epi_done;
           }
+          tc::fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
+          drain_chunk<EPI, EPI_COLS>(taddr, S);
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
+          acc_ph[buf] ^= 1;
+          buf ^= 1;
         }
         if (EPI == EPI_OZAKI) {
           if (row < p.m) {
@@ -628,14 +685,24 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
       }
       if (EPI == EPI_F32 && row < p.m) {
+        // C is read 8 columns at a time, every load of a group issued before
+        // the first use (one memory round trip per group, not per element)
         float* crow = p.c32 + row * p.rsc;
 #pragma unroll
-        for (int j = 0; j < EPI_COLS; ++j) {
-          const int64_t col = col0 + j;
-          if (col < p.n) {
-            float* cp = crow + col * p.csc;
-            const float v = (float)S[j] * p.alpha_f;
-            *cp = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, *cp, v);
+        for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
+          float c0[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t col = col0 + j0 + j;
+            c0[j] = (p.beta_f != 0.0f && col < p.n) ? crow[col * p.csc] : 0.0f;
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t col = col0 + j0 + j;
+            if (col < p.n) {
+              const float v = (float)S[j0 + j] * p.alpha_f;
+              crow[col * p.csc] = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, c0[j], v);
+            }
           }
         }
       }
@@ -656,6 +723,40 @@ __global__ void __launch_bounds__(THREADS, 1)
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+// Chunk counts of every group (Params::group_chunks) under the chunk rule
+// the MMA issuer applies step by step: a chunk takes a pair's k-blocks while
+// their weights fit in chunk_cap, continues into the next pair only with
+// merge_pairs, and a new chunk holds floor(chunk_cap / w) k-blocks of a pair
+// of weight w. Returns false if a weight exceeds the capacity.
+inline bool plan_chunks(Params& p) {
+  const int cap = p.chunk_cap;
+  for (int g = 0; g < p.ngroups; ++g) {
+    int n = 0, load = 0;
+    bool open = false;
+    for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
+      const int w = p.pair_w[pp];
+      if (w < 1 || w > cap) return false;
+      int rem = p.kblocks;
+      if (open && p.merge_pairs) {
+        const int take = std::min(rem, (cap - load) / w);
+        rem -= take;
+        load += take * w;
+      } else {
+        open = false;
+      }
+      if (rem > 0) {
+        const int per = cap / w;
+        const int fresh = (rem + per - 1) / per;
+        n += fresh;
+        load = (rem - (fresh - 1) * per) * w;
+        open = true;
+      }
+    }
+    p.group_chunks[g] = n;
+  }
+  return true;
+}
+
 template <int KIND, int EPI>
 inline cudaError_t set_slice_attrs() {
   cudaError_t e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, false>,
@@ -738,6 +839,7 @@ inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_f
                                                : (int64_t)p.tiles_m * p.tiles_n;
   const int64_t slots = v != SLICE_SINGLE ? clusters : sm_count;
   Params q = p;
+  if (!plan_chunks(q)) return cudaErrorInvalidValue;
   q.gchunk = p.ngroups;
   // Few tiles: a tile's accumulation groups (each writes its own int32 plane)
   // can run as separate work units. Pick the split whose schedule of units
