@@ -61,14 +61,6 @@ struct Epi {
 // and B, [operand][buffer][k][SROW_MAX] floats.
 constexpr int SMEM_BYTES = 2 * 2 * BK * SROW_MAX * 4;
 
-__device__ __forceinline__ void store_c(const Epi& e, int64_t row, int64_t col, float v) {
-  if (row < e.m && col < e.n) {
-    float* cp = e.c + row * e.rsc + col * e.csc;
-    float s = v * e.alpha;
-    *cp = (e.beta == 0.0f) ? s : fmaf(e.beta, *cp, s);
-  }
-}
-
 // This thread's share of one operand's k-block: two 4-element pieces, along
 // x (the non-k index) for an x-contiguous operand, along k otherwise. The
 // position is an element offset from the operand's base pointer, 32-bit when
@@ -211,15 +203,34 @@ __device__ __forceinline__ void ffma_unit_any(const Operands& o, int tm, int tn,
 __device__ __forceinline__ int64_t row_of(int tm, int i) { return (int64_t)tm * BM + row_in_tile(i); }
 __device__ __forceinline__ int64_t col_of(int tn, int j) { return (int64_t)tn * BN + col_in_tile(j); }
 
+// C = beta*C + alpha*v for the eight outputs of register row i: all loads of
+// C first, then the stores (one memory round trip per row, not per element).
+__device__ __forceinline__ void update_row(const Epi& e, int tm, int tn, int i, const float (&v)[8]) {
+  const int64_t row = row_of(tm, i);
+  float c0[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int64_t col = col_of(tn, j);
+    c0[j] = (e.beta != 0.0f && row < e.m && col < e.n) ? e.c[row * e.rsc + col * e.csc] : 0.0f;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int64_t col = col_of(tn, j);
+    if (row < e.m && col < e.n) {
+      const float t = v[j] * e.alpha;
+      e.c[row * e.rsc + col * e.csc] = (e.beta == 0.0f) ? t : fmaf(e.beta, c0[j], t);
+    }
+  }
+}
+
 // Epilogue; split-k partials are summed by the last split in split order.
+// Loads are issued a register row (8 values) at a time before any is used.
 __device__ __forceinline__ void ffma_finish(const Epi& e, float (&acc)[8][8], int tm, int tn, int splits, int sp,
                                             float* tile_partials, unsigned* counter, int* s_last) {
   const int tid = threadIdx.x;
   if (splits == 1) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) store_c(e, row_of(tm, i), col_of(tn, j), acc[i][j]);
+    for (int i = 0; i < 8; ++i) update_row(e, tm, tn, i, acc[i]);
     return;
   }
   const size_t tile_elems = (size_t)BM * BN;
@@ -238,14 +249,19 @@ __device__ __forceinline__ void ffma_finish(const Epi& e, float (&acc)[8][8], in
   if (*s_last) {
     __threadfence();
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 8; ++i) {
+      float v[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int r = (i * 8 + j) * THREADS + tid;
-        float s = __ldcg(tile_partials + r);
-        for (int q = 1; q < splits; ++q) s += __ldcg(tile_partials + (size_t)q * tile_elems + r);
-        store_c(e, row_of(tm, i), col_of(tn, j), s);
+      for (int j = 0; j < 8; ++j) v[j] = __ldcg(tile_partials + (i * 8 + j) * THREADS + tid);
+      for (int q = 1; q < splits; ++q) {
+        float w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = __ldcg(tile_partials + (size_t)q * tile_elems + (i * 8 + j) * THREADS + tid);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] += w[j];
       }
+      update_row(e, tm, tn, i, v);
+    }
     if (tid == 0) *counter = 0u;
   }
   __syncthreads();
