@@ -79,8 +79,10 @@ size_t work_bytes(int dtype, int precision, int slices, int64_t m, int64_t n, in
   if (precision == MOMMS_PREC_OZAKI) {
     const int s = slices > 0 ? slices : 8;  // FP64-level targets take up to 8 slices
     // digit planes of A and B, one int32 sum plane per accumulation group
+    // (tile-blocked: m and n padded to whole 128 x 256 tiles)
     const double groups = (double)ozaki_group_count(s, k);
-    bytes = 2.0 * s * (M + N) * (double)round_up(std::min<int64_t>(k, kOzakiMaxK), 8) + 4.0 * groups * M * N +
+    const double Mp = (double)round_up(m, 128), Np = (double)round_up(n, 256);
+    bytes = 2.0 * s * (M + N) * (double)round_up(std::min<int64_t>(k, kOzakiMaxK), 8) + 4.0 * groups * Mp * Np +
             12.0 * (M + N);
   } else if (precision == MOMMS_PREC_SPLIT_TF32) {
     bytes = 8.0 * (M + N) * (double)round_up(k, 4);

@@ -349,8 +349,9 @@ __global__ void __launch_bounds__(32) sample_final_kernel(const double* __restri
 // with R rounded to double once. All the summation is integer arithmetic;
 // FP64 is used for the final conversion, scaling and beta update only.
 struct CombineParams {
-  const int* sbuf;
+  const int* sbuf;  // tile-blocked group planes (sp::Params::sbuf)
   int64_t plane;
+  int64_t mpad;     // m rounded up to the slice kernel's tile height
   // Horner over the levels L = d_g - 2 <= dmax: entry q multiplies R by
   // 2^(bits * hsh[q]) and then adds group hg[q]'s S_g (hg[q] == 255: none).
   // Groups below dmax (lower diagonals; dmax = min(largest level, 12) keeps R below
@@ -420,18 +421,19 @@ constexpr int kCombineBatch = 16;  // Horner entries whose loads are issued toge
 __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
   constexpr int bits = kDigitBits;
   using u128 = unsigned __int128;
-  int64_t rows[2];
+  int64_t rows[2], roff[2];
   int er[2];
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     rows[u] = (int64_t)blockIdx.x * 512 + threadIdx.x + 256 * u;
     er[u] = rows[u] < p.m ? p.row_exp[rows[u]] : 0;
+    roff[u] = (rows[u] / sp::BM) * (sp::BM * sp::BN) + rows[u] % sp::BM;  // row's place in the tile blocks
   }
   if (rows[0] >= p.m) return;
   const bool two = rows[1] < p.m;
   for (int64_t j = p.j0 + blockIdx.y; j < p.j1; j += gridDim.y) {
     const int ec = p.col_exp[j];
-    const int* col = p.sbuf + j * p.m;
+    const int* col = p.sbuf + (j / sp::BN) * (p.mpad * sp::BN) + (j % sp::BN) * sp::BM;
     // two's complement in unsigned 128-bit arithmetic
     u128 R0 = 0, R1 = 0;
     if (p.nh <= kCombineBatch) {
@@ -443,8 +445,8 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
         s1[q] = 0;
         if (q < p.nh && p.hg[q] != 255) {
           const int* sg = col + (int64_t)p.hg[q] * p.plane;
-          s0[q] = sg[rows[0]];
-          if (two) s1[q] = sg[rows[1]];
+          s0[q] = sg[roff[0]];
+          if (two) s1[q] = sg[roff[1]];
         }
       }
 #pragma unroll
@@ -467,15 +469,15 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
         const int g = p.hg[q];
         if (g != 255) {
           const int* sg = col + (int64_t)g * p.plane;
-          R0 += (u128)(__int128)sg[rows[0]];
-          if (two) R1 += (u128)(__int128)sg[rows[1]];
+          R0 += (u128)(__int128)sg[roff[0]];
+          if (two) R1 += (u128)(__int128)sg[roff[1]];
         }
       }
     }
     for (int q = 0; q < p.ntail; ++q) {
       const int* sg = col + (int64_t)p.tail_g[q] * p.plane;
-      R0 += (u128)(__int128)(sg[rows[0]] >> p.tail_sh[q]);
-      if (two) R1 += (u128)(__int128)(sg[rows[1]] >> p.tail_sh[q]);
+      R0 += (u128)(__int128)(sg[roff[0]] >> p.tail_sh[q]);
+      if (two) R1 += (u128)(__int128)(sg[roff[1]] >> p.tail_sh[q]);
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -870,7 +872,10 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   call_info().groups = ng;
 
   int* sbuf = nullptr;
-  const size_t plane = (size_t)m * n;
+  // group planes tile-blocked (sp::Params::sbuf): m and n padded to whole
+  // 128 x 256 tiles, each tile one contiguous block
+  const int64_t mpad = round_up(m, (int64_t)sp::BM);
+  const size_t plane = (size_t)mpad * (size_t)round_up(n, (int64_t)sp::BN);
   if ((ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki group sums");
   p.plane = (int64_t)plane;
@@ -878,6 +883,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
 
   cp.sbuf = sbuf;
   cp.plane = (int64_t)plane;
+  cp.mpad = mpad;
   {
     // Horner entries in level order: a shift by one level between levels
     // (an empty level only shifts), then each group of the level
@@ -964,7 +970,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     }
     p.n = w;
     p.tiles_n = (int)ceil_div(w, sp::BN);
-    p.sbuf = sbuf + j0 * m;
+    p.sbuf = sbuf + j0 * mpad;  // j0 is a multiple of the tile width: the chunk's tile blocks start here
     {
       KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, X);
       int variant = 0;

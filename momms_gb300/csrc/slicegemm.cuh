@@ -87,7 +87,10 @@ struct Params {
   // EPI_F32
   float alpha_f, beta_f;
   float* c32;
-  // EPI_OZAKI: exact group sums, one column-major m x n int32 plane per group
+  // EPI_OZAKI: exact group sums, one int32 plane per group, tile-blocked:
+  // element (row, col) at (col / BN) * (tiles_m * BM * BN) + (row / BM) * BM * BN
+  // + (col % BN) * BM + row % BM, so that each CTA tile is written as one
+  // contiguous block
   int* sbuf;
   int64_t plane;
   int64_t rsc, csc;
@@ -382,11 +385,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (EPI == EPI_OZAKI) {
           // end of group g: publish the exact int32 sums (column-major plane g)
           if (row < p.m) {
-            int* srow = p.sbuf + (size_t)g * p.plane + row;
+            // tile-blocked plane: this CTA's 128 x 256 tile is one contiguous
+            // block, column after column of 128 rows (see the host's plane layout)
+            int* srow = p.sbuf + (size_t)g * p.plane + (size_t)tn * ((size_t)p.tiles_m * BM * BN) +
+                        (size_t)tm * (BM * BN) + (size_t)(h * EPI_COLS) * BM + r_local;
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) {
               const int64_t col = col0 + j;
-              if (col < p.n) srow[col * p.m] = S[j];
+              if (col < p.n) srow[j * BM] = S[j];
             }
           }
 #pragma unroll
@@ -673,11 +679,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         if (EPI == EPI_OZAKI) {
           if (row < p.m) {
-            int* srow = p.sbuf + (size_t)g * p.plane + row;
+            // tile-blocked plane: this CTA's 128 x 256 tile is one contiguous
+            // block, column after column of 128 rows (see the host's plane layout)
+            int* srow = p.sbuf + (size_t)g * p.plane + (size_t)tn * ((size_t)p.tiles_m * BM * BN) +
+                        (size_t)tm * (BM * BN) + (size_t)(h * EPI_COLS) * BM + r_local;
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) {
               const int64_t col = col0 + j;
-              if (col < p.n) srow[col * p.m] = S[j];
+              if (col < p.n) srow[j * BM] = S[j];
             }
           }
 #pragma unroll
