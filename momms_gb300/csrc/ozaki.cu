@@ -434,6 +434,13 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
   for (int64_t j = p.j0 + blockIdx.y; j < p.j1; j += gridDim.y) {
     const int ec = p.col_exp[j];
     const int* col = p.sbuf + (j / sp::BN) * (p.mpad * sp::BN) + (j % sp::BN) * sp::BM;
+    // C's old values are loaded with the group sums, not after the Horner
+    // steps, so a column costs one memory round trip
+    double c_old[2] = {0.0, 0.0};
+    if (!p.beta_zero) {
+      c_old[0] = p.c[rows[0] * p.rsc + j * p.csc];
+      if (two) c_old[1] = p.c[rows[1] * p.rsc + j * p.csc];
+    }
     // two's complement in unsigned 128-bit arithmetic
     u128 R0 = 0, R1 = 0;
     if (p.nh <= kCombineBatch) {
@@ -487,7 +494,7 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
       else v = i128_to_double((__int128)(u == 0 ? R0 : R1), er[u] + ec + p.scale_off);
       double* cp = p.c + rows[u] * p.rsc + j * p.csc;
       const double sv = p.alpha_one ? v : v * p.alpha;  // v * 1 == v: one FP64 operation saved
-      *cp = p.beta_zero ? sv : fma(p.beta, *cp, sv);
+      *cp = p.beta_zero ? sv : fma(p.beta, c_old[u], sv);
     }
   }
 }
