@@ -5,11 +5,11 @@
 // Every plain f64 problem contributes tiles x splits work units to one
 // persistent DMMA kernel and every plain f32 problem to one persistent FFMA
 // kernel. Units are ordered by decreasing cost (longest first) and handed to
-// the CTAs through a global atomic counter. The
-// split count of each problem is chosen so that no unit is much larger than
-// the batch's average share per SM (the runtime analogue of the reference's
-// compile-time block sizes); its k-splits are reduced in a fixed order, so a
-// problem's result does not depend on the rest of the batch.
+// the CTAs through a global atomic counter. Each problem keeps the split
+// count a single launch of its shape uses (the tuning table or the model,
+// tune.cu: the runtime analogue of the reference's compile-time block
+// sizes), and its k-splits are reduced in a fixed order, so a problem's
+// result does not depend on the rest of the batch.
 #include <string.h>
 
 #include <algorithm>
