@@ -1,10 +1,16 @@
 """Run one GEMM configuration repeatedly on the GPU (timing and profiling aid).
 
     python -m momms_gb300.run --m 4096 --n 4096 --k 4096 --dtype f64 --prec ozaki --reps 3
+    python -m momms_gb300.run --batched 512 --reps 5
 
 Operands are device-resident, column-major, uniform [-1, 1] from a fixed
 seed; C starts equal to A*B-sized random data and beta = 1. Prints one JSON
 line with the mean device time per call (CUDA events) and TFLOP/s.
+
+--batched N runs the uneven batch of the grouped-launch measurement instead:
+N problems with m, n, k log-uniform over [32, 1024] (numpy seed 512), half
+f64 and half f32, plain, as one execution plan launched through its CUDA
+graph.
 """
 import argparse
 import ctypes
@@ -26,7 +32,10 @@ def main():
     p.add_argument("--warmup", type=int, default=1)
     p.add_argument("--kernels", action="store_true",
                    help="also report each kernel class's mean time per call (CUDA events per launch)")
+    p.add_argument("--batched", type=int, default=0, help="time a plan of this many uneven problems instead")
     a = p.parse_args()
+    if a.batched:
+        return run_batched(a)
 
     import torch
     lib = mg.load_library()
@@ -79,6 +88,54 @@ def main():
         lib.momms_timing_enable(0)
         out["kernel_ms_per_call"] = per
     print(json.dumps(out))
+
+
+def run_batched(a):
+    """The grouped-launch batch: one plan, captured, relaunched `reps` times."""
+    import numpy as np
+    import torch
+    lib = mg.load_library()
+    rng = np.random.default_rng(512)
+    kinds = rng.choice(3, a.batched, p=[0.5, 0.0, 0.5])
+    dims = np.exp(rng.uniform(np.log(32), np.log(1024), (a.batched, 3))).astype(np.int64)
+    descs = (mg.GemmDesc * a.batched)()
+    keep = []
+    flops = 0.0
+    for i in range(a.batched):
+        m, n, k = (int(x) for x in dims[i])
+        dt = torch.float32 if kinds[i] == 2 else torch.float64
+        A = (torch.rand((k, m), dtype=dt, device="cuda") * 2 - 1).t()
+        B = (torch.rand((n, k), dtype=dt, device="cuda") * 2 - 1).t()
+        C = (torch.rand((n, m), dtype=dt, device="cuda") * 2 - 1).t()
+        d = mg.GemmDesc()
+        d.dtype = mg.DTYPE_F32 if kinds[i] == 2 else mg.DTYPE_F64
+        d.precision = mg.PREC_PLAIN
+        d.m, d.n, d.k = m, n, k
+        d.alpha, d.beta = 1.0, 1.0
+        d.a = mg.Operand(A.data_ptr(), 1, m, mg.MEM_DEVICE, 0)
+        d.b = mg.Operand(B.data_ptr(), 1, k, mg.MEM_DEVICE, 0)
+        d.c = mg.Operand(C.data_ptr(), 1, m, mg.MEM_DEVICE, 0)
+        descs[i] = d
+        keep.append((A, B, C))
+        flops += 2.0 * m * n * k
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    plan = ctypes.c_void_p()
+    mg.check(lib.momms_plan_create(descs, a.batched, ctypes.byref(plan)), lib)
+    mg.check(lib.momms_plan_capture(plan, sp), lib)
+    for _ in range(a.warmup):
+        mg.check(lib.momms_plan_launch(plan, sp), lib)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(a.reps):
+        mg.check(lib.momms_plan_launch(plan, sp), lib)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, a.reps)
+    lib.momms_plan_destroy(plan)
+    print(json.dumps({"batched": a.batched, "f64_problems": int((kinds != 2).sum()),
+                      "f32_problems": int((kinds == 2).sum()), "ms": ms,
+                      "tflops": flops / (ms * 1e-3) / 1e12}))
 
 
 if __name__ == "__main__":
