@@ -203,6 +203,20 @@ __device__ __forceinline__ void ffma_unit_any(const Operands& o, int tm, int tn,
 __device__ __forceinline__ int64_t row_of(int tm, int i) { return (int64_t)tm * BM + row_in_tile(i); }
 __device__ __forceinline__ int64_t col_of(int tn, int j) { return (int64_t)tn * BN + col_in_tile(j); }
 
+// Asks L2 for the C tile's lines when a unit starts (beta != 0), so that the
+// epilogue's loads of C hit L2: column-major C, 128 columns of four 128-byte
+// lines (32 rows each), two lines per thread. Other layouts are left to the
+// loads themselves.
+__device__ __forceinline__ void prefetch_c_tile(const Epi& e, int tm, int tn) {
+  if (e.beta == 0.0f || e.rsc != 1) return;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int line = (int)threadIdx.x + u * THREADS;  // 0..511
+    const int64_t row = (int64_t)tm * BM + (line & 3) * 32, col = (int64_t)tn * BN + (line >> 2);
+    if (row < e.m && col < e.n) asm volatile("prefetch.global.L2 [%0];" ::"l"(e.c + row + col * e.csc));
+  }
+}
+
 // C = beta*C + alpha*v for the eight outputs of register row i: all loads of
 // C first, then the stores (one memory round trip per row, not per element).
 __device__ __forceinline__ void update_row(const Epi& e, int tm, int tn, int i, const float (&v)[8]) {

@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(ffma::THREADS, 2)
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    prefetch_c_tile(P.e, tm, tn);
     ffma_unit_any<Off>(P.o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
     ffma_finish(P.e, acc, tm, tn, P.splits, sp,
                 P.splits > 1 ? partials + P.part_offset + (size_t)tile * P.splits * BM * BN : nullptr,

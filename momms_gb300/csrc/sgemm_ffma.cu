@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const __grid_constant
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    prefetch_c_tile(p.e, tm, tn);
     ffma_unit_t<A_XC, B_XC, Off>(o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
     if (SPLIT) {
       const int64_t tile = u / p.sched.splits;

@@ -140,6 +140,23 @@ __device__ __forceinline__ void drain_chunk(uint32_t taddr, EpiAcc<EPI> (&S)[NC]
   }
 }
 
+// Split-TF32 epilogue: asks L2 for the C lines this thread's warp will
+// read at the end of the tile (beta != 0), issued when the tile starts, so
+// that the epilogue's loads of C hit L2 instead of HBM. Column-major C: a
+// warp's 32 rows of one column are one 128-byte line, so lane L takes the
+// columns L, L + 32, ... of the thread's EPI_COLS; other layouts are left to
+// the loads themselves.
+template <int NC>
+__device__ __forceinline__ void prefetch_c_rows(const Params& p, int64_t row_of_lane0, int64_t col0, int lane) {
+  if (p.beta_f == 0.0f || p.rsc != 1 || row_of_lane0 >= p.m) return;
+  const float* base = p.c32 + row_of_lane0;
+#pragma unroll
+  for (int j = lane; j < NC; j += 32) {
+    const int64_t col = col0 + j;
+    if (col < p.n) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + col * p.csc));
+  }
+}
+
 template <int KIND, int EPI, bool MC>
 __global__ void __launch_bounds__(THREADS, 1)
     slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -360,6 +377,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       coords(t % tile_units, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
+      if (EPI == EPI_F32) prefetch_c_rows<EPI_COLS>(p, (int64_t)tm * BM + q * 32, col0, lane);
       // per-thread accumulators of finished chunks: exact int32 digit sums
       // (Ozaki) or FP32 sums rounded to nearest (split-TF32), which keeps the
       // tensor core's internal accumulation to one chunk at a time
@@ -658,6 +676,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       coords(t % tile_units, tm, tn);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
+      if (EPI == EPI_F32) prefetch_c_rows<EPI_COLS>(p, (int64_t)tm * BM + q * 32, col0, lane);
       EpiAcc<EPI> S[EPI_COLS];
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
