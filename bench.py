@@ -658,8 +658,7 @@ def run_ours(args):
                      "peak_source": f"bf16 dense cuBLAS {tc_peak_kind}, {peak_src} (fp16 and bf16 share the "
                                     "tcgen05 rate)",
                      "kernel": {2: "momms::sp::slice_gemm_pair_kernel<kind::f16, Ozaki> (cta_group::2 CTA pairs)",
-                                1: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki, multicast>",
-                                0: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>"}.get(info.multicast, "?"),
+                                0: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>"}.get(info.slice_variant, "?"),
                      "algorithmic_flops_per_launch": tc_flops_per_launch,
                      "kernel_ms_per_launch": slice_avg, "launches_per_step": slice_per_step,
                      "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps}},

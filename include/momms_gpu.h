@@ -122,13 +122,20 @@ int momms_sgemm(int64_t m, int64_t n, int64_t k, const float* alpha, const float
  * contents, so calls that overlap on the GPU (other streams, or other host
  * threads) race and must be serialised by the caller. The first call on each
  * device runs a one-time set-up with that device current (it looks up the
- * array's device address); make that first call before any stream capture.
- * A kernel whose bounded wait expires stops early without recording a status
- * here. Asynchronous on `stream`. */
+ * addresses of the array and of a status word); make that first call before
+ * any stream capture. A kernel whose bounded wait expires stops early, leaving
+ * C partly updated, and sets a bit in the no-alloc status word, a second
+ * device-global word of the library: momms_noalloc_status reads it. The
+ * operands must be memory of the current device. Asynchronous on `stream`. */
 #define MOMMS_NOALLOC_SCRATCH_BYTES 20975616
 int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a, int64_t rs_a,
                         int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, const double* beta, double* c,
                         int64_t rs_c, int64_t cs_c, void* stream);
+/* Reads and clears the current device's no-alloc status word (bits set by
+ * momms_dgemm_noalloc kernels whose bounded waits expired). Returns MOMMS_OK or
+ * MOMMS_ERR_DEVICE_TIMEOUT; *bits (if non-null) receives the raw word.
+ * Synchronises the device; allocates nothing. No reference counterpart. */
+int momms_noalloc_status(uint32_t* bits);
 
 /* ---- Packed operands --------------------------------------------------------
  * An operand used by many calls (a weight matrix, a basis) can be packed once
@@ -284,8 +291,8 @@ typedef struct {
   int32_t pairs;          /* OZAKI: slice products formed (tensor-core GEMMs) */
   int32_t groups;         /* OZAKI: accumulation groups */
   int32_t splits;         /* plain paths: k splits */
-  int32_t multicast;      /* tensor-core paths: slice kernel variant run: 0 = one CTA per tile, 1 = clusters
-                             of two sharing B tiles by multicast, 2 = CTA pairs with one cta_group::2 MMA */
+  int32_t slice_variant;  /* tensor-core paths: slice kernel variant run: 0 = one CTA per tile,
+                             2 = CTA pairs with one cta_group::2 MMA (1 is unused) */
   double bound_rel_err;   /* OZAKI: predicted worst-case |dC|/(|A||B|) */
 } momms_call_info;
 int momms_last_info(momms_call_info* out);
@@ -298,6 +305,30 @@ int momms_gemm_validate(const momms_gemm_desc* desc);
  * whose bounded waits expired). Returns MOMMS_OK or MOMMS_ERR_DEVICE_TIMEOUT;
  * *bits (if non-null) receives the raw word. Synchronises the device. */
 int momms_device_status(uint32_t* bits);
+
+/* Self-test of the bounded-wait failure path: launches one small kernel on
+ * `stream` that waits on a shared-memory barrier nothing arrives on, gives up
+ * after `polls` polls (1..2^20; the GEMM kernels allow 2^24, about a second),
+ * sets DEV_TIMEOUT_FULL (bit 0) in a status word and returns, so that the
+ * next momms_device_status (word 0) or momms_noalloc_status (word 1) reports
+ * MOMMS_ERR_DEVICE_TIMEOUT. The GPU context stays usable. No reference
+ * counterpart (the reference panics on the host, src/kern/ukernel_wrapper.rs:
+ * 23-28). */
+int momms_selftest_wait_expiry(uint32_t polls, int word, void* stream);
+
+/* Host-side fault injection for tests of the error paths: the library's next
+ * `count` operations of one kind fail as the real failure would be reported.
+ * MOMMS_FAULT_ALLOC: device allocations (scratch, staging buffers, packs,
+ * plans, autotuning) return out-of-memory; MOMMS_FAULT_CUDA: the check after
+ * a kernel launch reports a CUDA error (the launch itself has been made). The
+ * entry point that meets the fault returns MOMMS_ERR_OUT_OF_MEMORY or
+ * MOMMS_ERR_CUDA and releases what it holds, and later calls run normally.
+ * Process-wide; count 0 clears. No GPU fault is involved: the failure is
+ * reported, not caused. momms_fault_pending returns the faults of `kind` not
+ * yet used (-1 for an unknown kind). No reference counterpart. */
+typedef enum { MOMMS_FAULT_ALLOC = 0, MOMMS_FAULT_CUDA = 1 } momms_fault_kind;
+int momms_fault_inject(int kind, int count);
+int momms_fault_pending(int kind);
 
 /* Static description of the error codes, and the last error message of the
  * calling thread (empty string if none). */

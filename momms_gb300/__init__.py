@@ -32,6 +32,9 @@ KERNEL_SLICE_TF32 = 3
 KERNEL_PREP = 4
 KERNEL_COMBINE = 5
 
+FAULT_ALLOC = 0
+FAULT_CUDA = 1
+
 DTYPE_F64 = 0
 DTYPE_F32 = 1
 PREC_PLAIN = 0
@@ -61,7 +64,7 @@ class GemmDesc(ctypes.Structure):
 
 class CallInfo(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("slices", ctypes.c_int32), ("pairs", ctypes.c_int32),
-                ("groups", ctypes.c_int32), ("splits", ctypes.c_int32), ("multicast", ctypes.c_int32),
+                ("groups", ctypes.c_int32), ("splits", ctypes.c_int32), ("slice_variant", ctypes.c_int32),
                 ("bound_rel_err", ctypes.c_double)]
 
 
@@ -122,6 +125,14 @@ def load_library(path=None):
     lib.momms_dgemm_noalloc.restype = i32
     lib.momms_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
     lib.momms_device_status.restype = i32
+    lib.momms_noalloc_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    lib.momms_noalloc_status.restype = i32
+    lib.momms_selftest_wait_expiry.argtypes = [ctypes.c_uint32, i32, vp]
+    lib.momms_selftest_wait_expiry.restype = i32
+    lib.momms_fault_inject.argtypes = [i32, i32]
+    lib.momms_fault_inject.restype = i32
+    lib.momms_fault_pending.argtypes = [i32]
+    lib.momms_fault_pending.restype = i32
     lib.momms_status_string.argtypes = [i32]
     lib.momms_status_string.restype = ctypes.c_char_p
     lib.momms_last_error.argtypes = []

@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -21,6 +22,29 @@ DeviceState g_devices[64];
 }  // namespace
 
 momms_call_info& call_info() { return g_info; }
+
+namespace {
+std::atomic<int> g_fault_pending[2];
+}  // namespace
+
+bool fault_take(int kind) {
+  if (kind < 0 || kind > 1) return false;
+  int n = g_fault_pending[kind].load();
+  while (n > 0)
+    if (g_fault_pending[kind].compare_exchange_weak(n, n - 1)) return true;
+  return false;
+}
+
+cudaError_t device_malloc(void** ptr, size_t bytes) {
+  if (fault_take(MOMMS_FAULT_ALLOC)) return cudaErrorMemoryAllocation;
+  return cudaMalloc(ptr, bytes);
+}
+
+cudaError_t launch_status() {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && fault_take(MOMMS_FAULT_CUDA)) e = cudaErrorLaunchFailure;
+  return e;
+}
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -98,6 +122,7 @@ DeviceState* device_state() {
 }
 
 cudaError_t scratch_alloc_raw(void** ptr, size_t bytes, cudaStream_t s) {
+  if (fault_take(MOMMS_FAULT_ALLOC)) return cudaErrorMemoryAllocation;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
     cudaGetLastError();
@@ -163,7 +188,7 @@ int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, 
     repack_kernel<float><<<blocks, threads, 0, s>>>(static_cast<const float*>(src.ptr), src.rs, src.cs, rows, cols,
                                                      static_cast<float*>(dst), ld);
   note_launch();
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_status();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "repack");
 }
 
@@ -462,6 +487,19 @@ int momms_device_status(uint32_t* bits) {
   if (bits) *bits = w;
   if (w) return momms::fail(MOMMS_ERR_DEVICE_TIMEOUT, "device status bits 0x%x", w);
   return MOMMS_OK;
+}
+
+int momms_fault_inject(int kind, int count) {
+  if (kind != MOMMS_FAULT_ALLOC && kind != MOMMS_FAULT_CUDA)
+    return momms::fail(MOMMS_ERR_INVALID_ARG, "unknown fault kind %d", kind);
+  if (count < 0) return momms::fail(MOMMS_ERR_INVALID_ARG, "negative fault count");
+  momms::g_fault_pending[kind].store(count);
+  return MOMMS_OK;
+}
+
+int momms_fault_pending(int kind) {
+  if (kind != MOMMS_FAULT_ALLOC && kind != MOMMS_FAULT_CUDA) return -1;
+  return momms::g_fault_pending[kind].load();
 }
 
 const char* momms_status_string(int status) {

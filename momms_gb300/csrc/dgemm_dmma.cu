@@ -138,12 +138,14 @@ int set_attrs_dmma() {
   return MOMMS_OK;
 }
 
-int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
+namespace {
+// The launcher proper; scratch[0..2] (repacked A, B, split-k workspace) are
+// returned to the pool by the caller, on every path.
+int dgemm_dmma_impl(const DevGemm& g0, cudaStream_t s, void* (&scratch)[3]) {
   using namespace dmma;
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   DevGemm g = g0;
-  void* scratch[2] = {nullptr, nullptr};
   cudaError_t ce;
   if ((ce = wait_operands(g, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
 
@@ -215,7 +217,7 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
   call_info().splits = splits;
   p.partials = nullptr;
   p.counters = nullptr;
-  void* ws = nullptr;
+  void*& ws = scratch[2];
   if (splits > 1) {
     size_t part_bytes = (size_t)tiles * splits * BM * BN * 8;
     size_t cnt_bytes = (size_t)tiles * 4;
@@ -233,17 +235,24 @@ int launch_dgemm_dmma(const DevGemm& g0, cudaStream_t s) {
       kern<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
     }
     note_launch();
-    return cudaGetLastError();
+    return launch_status();
   };
   if (oa == ORIENT_XC && ob == ORIENT_XC) ce = launch(dgemm_kernel<true, true>);
   else if (oa == ORIENT_XC) ce = launch(dgemm_kernel<true, false>);
   else if (ob == ORIENT_XC) ce = launch(dgemm_kernel<false, true>);
   else ce = launch(dgemm_kernel<false, false>);
   if (ce != cudaSuccess) return cuda_fail(ce, "dgemm_dmma launch");
-  if (ws) cudaFreeAsync(ws, s);
+  return MOMMS_OK;
+}
+}  // namespace
+
+int launch_dgemm_dmma(const DevGemm& g, cudaStream_t s) {
+  void* scratch[3] = {nullptr, nullptr, nullptr};
+  const int rc = dgemm_dmma_impl(g, s, scratch);
+  // back to the pool in stream order, after the kernel if it was launched
   for (void* q : scratch)
     if (q) cudaFreeAsync(q, s);
-  return MOMMS_OK;
+  return rc;
 }
 
 }  // namespace momms
@@ -270,10 +279,15 @@ static_assert(kNoallocPartialBytes + kNoallocCounterSlots * sizeof(unsigned) == 
 // the same bytes. In host code this name is only a stand-in for the device
 // address: host code passes the address from cudaGetSymbolAddress instead.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MOMMS_NOALLOC_SCRATCH_BYTES];
+// The no-alloc calls' status word: a kernel whose bounded wait expires ORs a
+// DEV_* bit in here (momms_noalloc_status reads and clears it). Like the
+// scratch, one word per device for the life of the process.
+static __device__ unsigned g_noalloc_status;
 
 struct NoallocDevice {
   bool ready = false;
-  void* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+  void* scratch = nullptr;   // device address of g_noalloc_scratch on this device
+  unsigned* status = nullptr;  // device address of g_noalloc_status on this device
   int sm_count = 0;
 };
 std::mutex g_noalloc_mu;
@@ -293,6 +307,9 @@ int noalloc_setup(NoallocDevice*& out) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    void* st = nullptr;
+    e = cudaGetSymbolAddress(&st, g_noalloc_status);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc status)");
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
@@ -303,6 +320,7 @@ int noalloc_setup(NoallocDevice*& out) {
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
     }
     d.scratch = p;
+    d.status = static_cast<unsigned*>(st);
     d.sm_count = sms;
     d.ready = true;
   }
@@ -311,6 +329,13 @@ int noalloc_setup(NoallocDevice*& out) {
 }
 
 }  // namespace
+
+// The no-alloc status word of the current device (nullptr with the error
+// recorded if the set-up fails); used by the wait-expiry self-test.
+unsigned* noalloc_status_word() {
+  NoallocDevice* nd = nullptr;
+  return noalloc_setup(nd) ? nullptr : nd->status;
+}
 }  // namespace momms
 
 extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double* alpha, const double* a,
@@ -327,6 +352,11 @@ extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double
   if (rs_a < 0 || cs_a < 0 || rs_b < 0 || cs_b < 0 || rs_c < 0 || cs_c < 0)
     return fail(MOMMS_ERR_INVALID_ARG, "negative stride");
   if (m > 1 && n > 1 && rs_c == cs_c) return fail(MOMMS_ERR_INVALID_ARG, "C has equal strides");
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MOMMS_ERR_NO_DEVICE, "no current CUDA device");
+  }
   const void* ptrs[3] = {a, b, c};
   for (const void* p : ptrs) {
     cudaPointerAttributes at;
@@ -336,6 +366,10 @@ extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double
       return fail(MOMMS_ERR_INVALID_ARG,
                   "momms_dgemm_noalloc takes device operands only (staging host memory would allocate)");
     }
+    // the kernels' TMA reads go to this device's memory only
+    if (at.type == cudaMemoryTypeDevice && at.device != cur)
+      return fail(MOMMS_ERR_INVALID_ARG, "operand is memory of device %d, the current device is %d", at.device,
+                  cur);
   }
   NoallocDevice* nd = nullptr;
   int rc = noalloc_setup(nd);
@@ -391,7 +425,7 @@ extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double
   p.alpha = g.alpha; p.beta = g.beta;
   p.c = c;
   p.rsc = rs_c; p.csc = cs_c;
-  p.status = nullptr;  // no status word here: that one is allocated on first use
+  p.status = nd->status;  // the no-alloc status word, not the library's allocated one
   const int tiles_m = (int)ceil_div(g.m, BM), tiles_n = (int)ceil_div(g.n, BN);
   const int64_t tiles = (int64_t)tiles_m * tiles_n;
   const int64_t kblocks = ceil_div(g.k, BK);
@@ -419,7 +453,24 @@ extern "C" int momms_dgemm_noalloc(int64_t m, int64_t n, int64_t k, const double
   else if (ob == ORIENT_XC) dgemm_kernel<false, true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
   else dgemm_kernel<false, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
   note_launch();
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_status();
   if (e != cudaSuccess) return cuda_fail(e, "dgemm_noalloc launch");
+  return MOMMS_OK;
+}
+
+extern "C" int momms_noalloc_status(uint32_t* bits) {
+  using namespace momms;
+  NoallocDevice* nd = nullptr;
+  int rc = noalloc_setup(nd);
+  if (rc) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+  unsigned w = 0;
+  const unsigned zero = 0;
+  e = cudaMemcpyFromSymbol(&w, g_noalloc_status, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_noalloc_status, &zero, sizeof(unsigned));
+  if (e != cudaSuccess) return cuda_fail(e, "no-alloc status word");
+  if (bits) *bits = w;
+  if (w) return fail(MOMMS_ERR_DEVICE_TIMEOUT, "no-alloc status bits 0x%x", w);
   return MOMMS_OK;
 }

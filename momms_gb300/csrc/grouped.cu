@@ -268,7 +268,7 @@ int plan_alloc(Plan* p, void** out, size_t bytes) {
     *out = nullptr;
     return MOMMS_OK;
   }
-  cudaError_t e = p->async ? scratch_alloc(out, bytes, p->stream) : cudaMalloc(out, bytes);
+  cudaError_t e = p->async ? scratch_alloc(out, bytes, p->stream) : device_malloc(out, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "plan allocation");
   p->allocs.push_back(*out);
   return MOMMS_OK;
@@ -590,7 +590,7 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     grouped::dgemm_grouped_kernel<<<grid, dmma::THREADS, dmma::SMEM_BYTES, s>>>(
         p->d_maps, p->d_probs, p->nd, p->d_units, p->d_partials, p->d_counters, p->d_next, ds->status);
     note_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f64 launch");
+    if ((e = launch_status()) != cudaSuccess) return cuda_fail(e, "grouped f64 launch");
   }
   if (p->ns) {
     const int sms = (max_sms > 0 && max_sms < ds->sm_count) ? max_sms : ds->sm_count;
@@ -603,7 +603,7 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
       grouped::sgemm_grouped_kernel<uint32_t><<<grid, ffma::THREADS, ffma::SMEM_BYTES, s>>>(p->s_probs, p->ns, p->s_units,
                                                                            p->s_next, p->s_partials, p->s_counters);
     note_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
+    if ((e = launch_status()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
   }
   for (PlanProblem& pp : p->other) {
     const DevGemm g = devgemm_of(pp.d);

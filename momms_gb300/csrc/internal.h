@@ -32,9 +32,31 @@ inline cudaError_t scratch_alloc(T** ptr, size_t bytes, cudaStream_t s) {
   return scratch_alloc_raw(reinterpret_cast<void**>(ptr), bytes, s);
 }
 
+// Returns a stream-ordered scratch allocation to the pool, in order on `s`,
+// when it goes out of scope: on every return path of a launcher.
+struct ScratchGuard {
+  void* p;
+  cudaStream_t s;
+  ScratchGuard(void* ptr, cudaStream_t st) : p(ptr), s(st) {}
+  ~ScratchGuard() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  ScratchGuard(const ScratchGuard&) = delete;
+  ScratchGuard& operator=(const ScratchGuard&) = delete;
+};
+
 // Returns the state of the calling thread's current device (initialising it
 // on first use), or nullptr with the error recorded.
 DeviceState* device_state();
+
+// ---- Host-side fault injection (momms_fault_inject) ----
+// fault_take(kind) is true, using up one pending fault, when the next
+// operation of that kind is to fail. device_malloc is cudaMalloc with
+// injected out-of-memory failures; launch_status is the check made after a
+// kernel launch (cudaGetLastError) with injected CUDA errors.
+bool fault_take(int kind);
+cudaError_t device_malloc(void** ptr, size_t bytes);
+cudaError_t launch_status();
 
 // Record an error message for momms_last_error() and return `code`.
 int fail(int code, const char* fmt, ...);

@@ -563,7 +563,7 @@ int ozaki_operand_exponents(const double* x, int64_t sr, int64_t sp, int64_t R, 
       x, sr, sp, R, K, r_contig, maxbits);
   exps_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, s>>>(maxbits, R, exps);
   note_launch(2);
-  ce = cudaGetLastError();
+  ce = launch_status();
   return ce == cudaSuccess ? MOMMS_OK : cuda_fail(ce, "Ozaki exponents");
 }
 
@@ -807,6 +807,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   void* ebuf = nullptr;
   if ((ce = scratch_alloc(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki exponents");
+  ScratchGuard free_ebuf(ebuf, s);
   unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
   int* exps = reinterpret_cast<int*>(maxbits + (m + n));
   const double* A = static_cast<const double*>(g.a.ptr);
@@ -841,6 +842,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const size_t own = (PA ? 0 : (size_t)ns * a_plane) + (PB ? 0 : (size_t)ns * b_plane);
   if (own && (ce = scratch_alloc(&planes_buf, own * sizeof(__half), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki slice planes");
+  ScratchGuard free_planes(planes_buf, s);
   const __half* pa = PA ? static_cast<const __half*>(PA->planes) : planes_buf;
   const __half* pb = PB ? static_cast<const __half*>(PB->planes) : planes_buf + (PA ? 0 : (size_t)ns * a_plane);
   if (!PA) ozaki_operand_planes(ns, A, g.a.rs, g.a.cs, m, k, const_cast<__half*>(pa), kp, rexp, s);
@@ -885,6 +887,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const size_t plane = (size_t)mpad * (size_t)round_up(n, (int64_t)sp::BN);
   if ((ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki group sums");
+  ScratchGuard free_sbuf(sbuf, s);
   p.plane = (int64_t)plane;
   p.status = ds->status;
 
@@ -970,7 +973,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pbc, dimsb, stridesb, boxb,
                         CU_TENSOR_MAP_SWIZZLE_128B);
       if (rc) break;
-      uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
+      uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};  // one CTA's half of the B tile for the pair kernel
       rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pbc, dimsb, stridesb, boxh,
                         CU_TENSOR_MAP_SWIZZLE_128B);
       if (rc) break;
@@ -982,11 +985,12 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, X);
       int variant = 0;
       ce = sp::launch_slice<0, sp::EPI_OZAKI>(tmA, tmB, tmB_half, p, ds->sm_count, X, &variant);
+      if (ce == cudaSuccess) ce = launch_status();
       if (ce != cudaSuccess) {
         rc = cuda_fail(ce, "Ozaki slice launch");
         break;
       }
-      call_info().multicast = variant;
+      call_info().slice_variant = variant;
     }
     note_launch();
     // C's columns j0..j1: recombination; with C staged from host memory and
@@ -1008,7 +1012,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
         combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, X>>>(cp);
       }
       note_launch();
-      ce = cudaGetLastError();
+      ce = launch_status();
       if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki launch");
       if (!rc) rc = columns_done(g, cp.j0, cp.j1, X);
     }
@@ -1022,10 +1026,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     cudaEventDestroy(ev_fork);
     cudaEventDestroy(ev_join);
   }
-  if (planes_buf) cudaFreeAsync(planes_buf, s);
-  cudaFreeAsync(sbuf, s);
-  cudaFreeAsync(ebuf, s);
-  return rc;
+  return rc;  // the guards return the scratch to the pool, in order on s after the join
 }
 
 }  // namespace momms

@@ -29,6 +29,16 @@ int check_packed(const momms_gemm_desc& d, int which, const PackedOperand* p) {
   const char name = which == 0 ? 'A' : 'B';
   if (!pack_is_live(p)) return fail(MOMMS_ERR_INVALID_ARG, "%c is not a live packed operand", name);
   if (p->role != which) return fail(MOMMS_ERR_INVALID_ARG, "%c: the pack was made for the other operand", name);
+  // a pack is memory of the device it was made on; the kernels (TMA loads
+  // included) may read only the current device's memory
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MOMMS_ERR_NO_DEVICE, "no current CUDA device");
+  }
+  if (p->device != dev)
+    return fail(MOMMS_ERR_INVALID_ARG, "%c: the pack lives on device %d, the call runs on device %d", name, p->device,
+                dev);
   const int64_t rows = which == 0 ? d.m : d.k, cols = which == 0 ? d.k : d.n;
   if (p->rows != rows || p->cols != cols)
     return fail(MOMMS_ERR_INVALID_ARG, "%c: pack is %lld x %lld, the call needs %lld x %lld", name,
@@ -118,7 +128,7 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
   if (precision == MOMMS_PREC_PLAIN) {
     p->ld = round_up(rows, 16 / (int64_t)es);
     p->bytes = (size_t)p->ld * (size_t)cols * es;
-    ce = cudaMalloc(&p->mem, p->bytes);
+    ce = device_malloc((void**)&p->mem, p->bytes);
     if (ce == cudaSuccess) {
       p->data = p->mem;
       rc = repack_colmajor(v, rows, cols, es, p->data, p->ld, s);
@@ -129,7 +139,7 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
     const size_t plane_bytes = (size_t)p->np * (size_t)R * (size_t)p->kp * 2;
     const size_t exps_off = round_up((int64_t)plane_bytes, 256);
     p->bytes = exps_off + (size_t)round_up((int64_t)((size_t)R * sizeof(int)), 8) + (size_t)R * sizeof(unsigned long long);
-    ce = cudaMalloc(&p->mem, p->bytes);
+    ce = device_malloc((void**)&p->mem, p->bytes);
     if (ce == cudaSuccess) {
       p->planes = p->mem;
       p->exps = reinterpret_cast<int*>(static_cast<char*>(p->mem) + exps_off);
@@ -144,14 +154,14 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
     p->np = 2;
     p->kp = round_up(K, 4);
     p->bytes = 2 * (size_t)R * (size_t)p->kp * 4;
-    ce = cudaMalloc(&p->mem, p->bytes);
+    ce = device_malloc((void**)&p->mem, p->bytes);
     if (ce == cudaSuccess) {
       p->planes = p->mem;
       const int64_t sr = role == MOMMS_ROLE_A ? v.rs : v.cs, sp = role == MOMMS_ROLE_A ? v.cs : v.rs;
       tf32_operand_planes(static_cast<const float*>(v.ptr), sr, sp, R, K, static_cast<float*>(p->planes), p->kp, s);
     }
   }
-  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce == cudaSuccess) ce = launch_status();
   if (st.owned) cudaFreeAsync(st.owned, s);
   cudaError_t e2 = cudaStreamSynchronize(s);
   if (!rc && ce != cudaSuccess) rc = cuda_fail(ce, "pack");

@@ -64,7 +64,7 @@ int momms_measure_peak(int kind, double* tflops) {
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   const int blocks = ds->sm_count * 4, threads = 256;
   void* out = nullptr;
-  cudaError_t e = cudaMalloc(&out, (size_t)blocks * threads * sizeof(double));
+  cudaError_t e = device_malloc((void**)&out, (size_t)blocks * threads * sizeof(double));
   if (e != cudaSuccess) return cuda_fail(e, "peak probe buffer");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

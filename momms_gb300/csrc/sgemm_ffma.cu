@@ -58,12 +58,14 @@ __global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const __grid_constant
 
 }  // namespace ffma
 
-int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
+namespace {
+// The launcher proper; scratch[0..2] (repacked A, B, split-k workspace) are
+// returned to the pool by the caller, on every path.
+int sgemm_ffma_impl(const DevGemm& g0, cudaStream_t s, void* (&scratch)[3]) {
   using namespace ffma;
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   DevGemm g = g0;
-  void* scratch[2] = {nullptr, nullptr};
   cudaError_t ce;
   if ((ce = wait_operands(g, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
   // A must have unit stride along m or k; B along k or n. Anything else is
@@ -107,7 +109,7 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
   call_info().splits = splits;
   p.partials = nullptr;
   p.counters = nullptr;
-  void* ws = nullptr;
+  void*& ws = scratch[2];
   if (splits > 1) {
     size_t part_bytes = (size_t)tiles * splits * BM * BN * 4;
     size_t cnt_bytes = (size_t)tiles * 4;
@@ -134,12 +136,18 @@ int launch_sgemm_ffma(const DevGemm& g0, cudaStream_t s) {
     k<<<grid, THREADS, SMEM_BYTES, s>>>(p);
   }
   note_launch();
-  ce = cudaGetLastError();
+  ce = launch_status();
   if (ce != cudaSuccess) return cuda_fail(ce, "sgemm_ffma launch");
-  if (ws) cudaFreeAsync(ws, s);
+  return MOMMS_OK;
+}
+}  // namespace
+
+int launch_sgemm_ffma(const DevGemm& g, cudaStream_t s) {
+  void* scratch[3] = {nullptr, nullptr, nullptr};
+  const int rc = sgemm_ffma_impl(g, s, scratch);
   for (void* q : scratch)
     if (q) cudaFreeAsync(q, s);
-  return MOMMS_OK;
+  return rc;
 }
 
 }  // namespace momms

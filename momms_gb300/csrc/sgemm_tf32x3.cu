@@ -60,6 +60,7 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
   const size_t own = (PA ? 0 : 2 * a_plane) + (PB ? 0 : 2 * b_plane);
   if (own && (ce = scratch_alloc(&buf, own * sizeof(float), s)) != cudaSuccess)
     return cuda_fail(ce, "split-TF32 planes");
+  ScratchGuard free_buf(buf, s);
   float* pa = PA ? static_cast<float*>(PA->planes) : static_cast<float*>(buf);
   float* pb = PB ? static_cast<float*>(PB->planes) : static_cast<float*>(buf) + (PA ? 0 : 2 * a_plane);
   // each operand's split waits only for that operand
@@ -84,7 +85,7 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
     uint32_t boxb[3] = {32, (uint32_t)sp::BN, 1};
     rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pb, dimsb, stridesb, boxb, CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
-    uint32_t boxh[3] = {32, (uint32_t)(sp::BN / 2), 1};  // one CTA's half for the multicast kernel
+    uint32_t boxh[3] = {32, (uint32_t)(sp::BN / 2), 1};  // one CTA's half of the B tile for the pair kernel
     rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, pb, dimsb, stridesb, boxh,
                       CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc) return rc;
@@ -124,12 +125,11 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s) {
     int variant = 0;
     ce = sp::launch_slice<1, sp::EPI_F32>(tmA, tmB, tmB_half, p, ds->sm_count, s, &variant);
     if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 slice launch");
-    call_info().multicast = variant;
+    call_info().slice_variant = variant;
   }
   note_launch();
-  ce = cudaGetLastError();
+  ce = launch_status();
   if (ce != cudaSuccess) return cuda_fail(ce, "split-TF32 launch");
-  if (buf) cudaFreeAsync(buf, s);
   return MOMMS_OK;
 }
 

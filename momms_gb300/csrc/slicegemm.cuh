@@ -13,15 +13,6 @@
 // memory descriptors expect. Warp roles: warp 0 issues TMA, warp 1 (one
 // thread) issues tcgen05.mma and commits, warps 2..9 drain TMEM.
 //
-// Multicast variant (MC): CTAs run in clusters of two on vertically adjacent
-// output tiles (tm = 2 * pair + rank, same tn), which read the same B tile.
-// Each CTA loads its own A tile and one half of the B tile, multicast into
-// both CTAs' shared memory, so a stage costs each SM two thirds of the L2
-// reads; each CTA's MMA thread releases a stage in both CTAs
-// (empty barriers count two arrivals), since the peer's next multicast
-// writes into it. A cluster barrier after initialisation and before exit
-// keeps every remote write and arrival inside the lifetime of its target.
-//
 // Two epilogues:
 //   EPI_F32   : one group; finished chunks are summed in FP32 registers
 //               (round to nearest) and C = alpha*sum + beta*C is written at
@@ -157,7 +148,7 @@ __device__ __forceinline__ void prefetch_c_rows(const Params& p, int64_t row_of_
   }
 }
 
-template <int KIND, int EPI, bool MC>
+template <int KIND, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ Params p) {
@@ -172,11 +163,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // work units: output tiles, or (MC) vertical tile pairs, one per cluster
-  const uint32_t rank = MC ? cluster_ctarank() : 0u;
-  const int64_t unit0 = MC ? (int64_t)cluster_id_x() : (int64_t)blockIdx.x;
-  const int64_t unit_step = MC ? (int64_t)cluster_count_x() : (int64_t)gridDim.x;
-  const int units_m = MC ? (p.tiles_m + 1) / 2 : p.tiles_m;
+  // work units: output tiles (times group chunks), one CTA each
+  const int64_t unit0 = (int64_t)blockIdx.x;
+  const int64_t unit_step = (int64_t)gridDim.x;
+  const int units_m = p.tiles_m;
   // work unit t: tile (pair) t % tile_units, groups [g_begin(t), g_end(t)) -
   // group-major, so that units in flight read the same digit planes
   const int64_t tile_units = (int64_t)units_m * p.tiles_n;
@@ -190,16 +180,12 @@ __global__ void __launch_bounds__(THREADS, 1)
   auto unit_at = [&](int64_t r) {
     return r * unit_step + ((r & 1) ? (unit_step - 1 - unit0) : unit0);
   };
-  auto coords = [&](int64_t t, int& tm, int& tn) {
-    int um;
-    tile_coords<MC ? 8 : 16>(t, units_m, p.tiles_n, um, tn);
-    tm = MC ? 2 * um + (int)rank : um;  // MC: rank 1 of an odd last pair reads zero rows, writes nothing
-  };
+  auto coords = [&](int64_t t, int& tm, int& tn) { tile_coords<16>(t, units_m, p.tiles_n, tm, tn); };
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&empty[i], MC ? 2 : 1);
+      mbar_init(&empty[i], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
@@ -215,7 +201,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   tc::fence_before();
   __syncthreads();
-  if (MC) cluster_sync();  // the peer's barriers exist before any multicast reaches them
   tc::fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
@@ -249,31 +234,12 @@ __global__ void __launch_bounds__(THREADS, 1)
               mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
               uint8_t* sa = smem + stage * STAGE_BYTES;
               tma_load_3d(sa, &tmA, &full[stage], kb * p.kelems, tm * BM, p.pair_a[pi]);
-              if (MC)  // this CTA's half of the B tile, into both CTAs (its tmB box is BN/2 rows)
-                tma_load_3d_mc(sa + A_TILE + rank * (B_TILE / 2), &tmB, &full[stage], kb * p.kelems,
-                               tn * BN + (int)rank * (BN / 2), p.pair_b[pi], (uint16_t)0x3);
-              else
-                tma_load_3d(sa + A_TILE, &tmB, &full[stage], kb * p.kelems, tn * BN, p.pair_b[pi]);
+              tma_load_3d(sa + A_TILE, &tmB, &full[stage], kb * p.kelems, tn * BN, p.pair_b[pi]);
               if (++stage == STAGES) {
                 stage = 0;
                 ph ^= 1;
               }
             }
-          }
-        }
-      }
-      if (MC && !aborted(abort_flag)) {
-        // every stage released by both CTAs: no arrival from the peer is
-        // still on its way to this CTA's barriers
-        for (int i = 0; i < STAGES; ++i) {
-          if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
-            report_status(p.status, DEV_TIMEOUT_EMPTY);
-            *abort_flag = 1;
-            break;
-          }
-          if (++stage == STAGES) {
-            stage = 0;
-            ph ^= 1;
           }
         }
       }
@@ -336,10 +302,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 for (int kk = 0; kk < KSTEPS; ++kk)
                   tc::mma<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
                                 (fresh && st == s0 && kk == 0) ? 0u : 1u);
-                if (MC)
-                  tc::commit_mc(&empty[stage], (uint16_t)0x3);  // both CTAs' copies of the stage are free
-                else
-                  tc::commit(&empty[stage]);
+                tc::commit(&empty[stage]);
                 if (++stage == STAGES) {
                   stage = 0;
                   ph ^= 1;
@@ -448,7 +411,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncwarp();
   tc::fence_before();
   __syncthreads();
-  if (MC) cluster_sync();  // the peer is done writing into this CTA
   if (warp == 1) {
     tc::fence_after();
     tc::tmem_dealloc(tmem_base, TMEM_COLS);
@@ -787,22 +749,19 @@ inline bool plan_chunks(Params& p) {
 
 template <int KIND, int EPI>
 inline cudaError_t set_slice_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             SMEM_BYTES);
+  cudaError_t e = cudaFuncSetAttribute(slice_gemm_kernel<KIND, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       SMEM_BYTES);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(slice_gemm_pair_kernel<KIND, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              P_SMEM_BYTES);
   return e;
 }
 
-// Kernel variants: 0 = one CTA per tile, 1 = clusters of two with B
-// multicast, 2 = CTA pairs with cta_group::2 MMA.
-enum { SLICE_SINGLE = 0, SLICE_MULTICAST = 1, SLICE_PAIR = 2 };
+// Kernel variants: 0 = one CTA per tile, 2 = CTA pairs with cta_group::2 MMA
+// (1 is not used: it was a cluster kernel sharing B tiles by multicast loads).
+enum { SLICE_SINGLE = 0, SLICE_PAIR = 2 };
 
-inline cudaLaunchConfig_t cluster2_config(const void*, int smem, cudaLaunchAttribute* attr) {
+inline cudaLaunchConfig_t cluster2_config(int smem, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2);
   cfg.blockDim = dim3(THREADS);
@@ -816,9 +775,10 @@ inline cudaLaunchConfig_t cluster2_config(const void*, int smem, cudaLaunchAttri
   return cfg;
 }
 
-// The variant to use on the current device and how many clusters of two fit
-// at once; queried once per device. MOMMS_SLICE_VARIANT=0/1/2 restricts the
-// choice to at most that variant (default: the pair kernel).
+// The variant to use on the current device and how many CTA pairs fit at
+// once; queried once per device. MOMMS_SLICE_VARIANT=0 restricts the choice to
+// the single-CTA kernel (default and MOMMS_SLICE_VARIANT=2: the pair kernel
+// wherever the device can co-schedule pairs).
 template <int KIND, int EPI>
 inline int slice_variant(int* clusters) {
   static std::atomic<int> cache_v[64], cache_n[64];
@@ -827,22 +787,19 @@ inline int slice_variant(int* clusters) {
   *clusters = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SLICE_SINGLE;
   if (!init[dev].load()) {
-    int want = SLICE_PAIR;
     const char* env = getenv("MOMMS_SLICE_VARIANT");
-    if (env && env[0] >= '0' && env[0] <= '2') want = env[0] - '0';
+    const bool want_pair = !(env && env[0] == '0');
     int v = SLICE_SINGLE, n = 0;
-    for (int cand = want; cand >= SLICE_MULTICAST && v == SLICE_SINGLE; --cand) {
+    if (want_pair) {
       cudaLaunchAttribute attr[1];
-      const void* fn = cand == SLICE_PAIR ? (const void*)slice_gemm_pair_kernel<KIND, EPI>
-                                          : (const void*)slice_gemm_kernel<KIND, EPI, true>;
-      cudaLaunchConfig_t cfg = cluster2_config(fn, cand == SLICE_PAIR ? P_SMEM_BYTES : SMEM_BYTES, attr);
+      cudaLaunchConfig_t cfg = cluster2_config(P_SMEM_BYTES, attr);
       int c = 0;
-      if (cudaOccupancyMaxActiveClusters(&c, fn, &cfg) != cudaSuccess) {
+      if (cudaOccupancyMaxActiveClusters(&c, (const void*)slice_gemm_pair_kernel<KIND, EPI>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         c = 0;
       }
       if (c > 0) {
-        v = cand;
+        v = SLICE_PAIR;
         n = c;
       }
     }
@@ -854,18 +811,19 @@ inline int slice_variant(int* clusters) {
   return cache_v[dev].load();
 }
 
-// Launches the slice kernel. The cluster variants need at least two m-tiles
-// (their units are vertical tile pairs) and take tmB_half, whose box is BN/2
-// rows; the single-CTA kernel takes tmB_full. *variant receives the one run.
+// Launches the slice kernel. The pair kernel needs at least two m-tiles (its
+// units are vertical tile pairs) and takes tmB_half, whose box is BN/2 rows
+// (each CTA of a pair stages its half of the B tile); the single-CTA kernel
+// takes tmB_full. *variant receives the one run.
 template <int KIND, int EPI>
 inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_full, const CUtensorMap& tmB_half,
                                 const Params& p, int sm_count, cudaStream_t s, int* variant) {
   int clusters = 0;
   const int v = p.tiles_m >= 2 ? slice_variant<KIND, EPI>(&clusters) : SLICE_SINGLE;
   *variant = v;
-  const int64_t tile_units = v != SLICE_SINGLE ? (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n
-                                               : (int64_t)p.tiles_m * p.tiles_n;
-  const int64_t slots = v != SLICE_SINGLE ? clusters : sm_count;
+  const int64_t tile_units = v == SLICE_PAIR ? (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n
+                                             : (int64_t)p.tiles_m * p.tiles_n;
+  const int64_t slots = v == SLICE_PAIR ? clusters : sm_count;
   Params q = p;
   if (!plan_chunks(q)) return cudaErrorInvalidValue;
   q.gchunk = p.ngroups;
@@ -896,18 +854,15 @@ inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_f
     }
   }
   const int64_t units = tile_units * ((p.ngroups + q.gchunk - 1) / q.gchunk);
-  if (v != SLICE_SINGLE) {
+  if (v == SLICE_PAIR) {
     cudaLaunchAttribute attr[1];
-    const void* fn = v == SLICE_PAIR ? (const void*)slice_gemm_pair_kernel<KIND, EPI>
-                                     : (const void*)slice_gemm_kernel<KIND, EPI, true>;
-    cudaLaunchConfig_t cfg = cluster2_config(fn, v == SLICE_PAIR ? P_SMEM_BYTES : SMEM_BYTES, attr);
+    cudaLaunchConfig_t cfg = cluster2_config(P_SMEM_BYTES, attr);
     cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
     cfg.stream = s;
-    if (v == SLICE_PAIR) return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, q);
-    return cudaLaunchKernelEx(&cfg, slice_gemm_kernel<KIND, EPI, true>, tmA, tmB_half, q);
+    return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, q);
   }
   const int grid = (int)std::min<int64_t>(units, sm_count);
-  slice_gemm_kernel<KIND, EPI, false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, q);
+  slice_gemm_kernel<KIND, EPI><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, q);
   return cudaGetLastError();
 }
 

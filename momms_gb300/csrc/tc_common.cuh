@@ -76,16 +76,6 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
                : "memory");
 }
 
-// Same, arriving on the mbarrier at `bar`'s offset in every CTA of the
-// cluster in `mask`.
-__device__ __forceinline__ void commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(mask)
-      : "memory");
-}
-
 // ---- CTA pairs (cta_group::2): one MMA spans the TMEM of both CTAs of a
 // cluster of two. Every tcgen05 instruction of such a kernel uses
 // cta_group::2. The allocation is collective: warp 1 of both CTAs executes it

@@ -86,7 +86,7 @@ int momms_autotune(const momms_gemm_desc* desc, momms_tune_result* out, void* st
   const int64_t kblocks = ceil_div(desc->k, bk);
   // scratch C so that the caller's C is not touched
   void* cs = nullptr;
-  cudaError_t e = cudaMalloc(&cs, (size_t)desc->m * desc->n * es);
+  cudaError_t e = device_malloc((void**)&cs, (size_t)desc->m * desc->n * es);
   if (e != cudaSuccess) return cuda_fail(e, "autotune scratch");
   momms_gemm_desc d = *desc;
   d.c = momms_operand{cs, 1, desc->m, MOMMS_MEM_DEVICE, 0};

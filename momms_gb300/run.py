@@ -69,7 +69,7 @@ def main():
     lib.momms_last_info(ctypes.byref(info))
     out = {"m": a.m, "n": a.n, "k": a.k, "dtype": a.dtype, "prec": a.prec, "ms": ms,
            "tflops": 2.0 * a.m * a.n * a.k / (ms * 1e-3) / 1e12, "slices": info.slices,
-           "pairs": info.pairs, "splits": info.splits, "slice_variant": info.multicast}
+           "pairs": info.pairs, "splits": info.splits, "slice_variant": info.slice_variant}
     if a.kernels:
         # separate timed pass: per-launch events would perturb the whole-call time above
         lib.momms_timing_enable(1)

@@ -10,6 +10,11 @@
   compiled unmodified from the reference checkout with a typedef-only
   ``blis.h`` stub. x86-64 only (the kernels are AVX2/FMA inline assembly) and
   only where the reference checkout exists; everywhere else it is skipped.
+
+Where the checkout is: the directory named by ``--reference DIR`` (when run
+as a script) or the ``MOMMS_REFERENCE_ROOT`` environment variable; unset, a
+``reference`` directory beside the repository (``../reference`` from its
+root) if one is there. With none of these the reference build is skipped.
 """
 import os
 import platform
@@ -17,7 +22,18 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REPO_ROOT = os.path.dirname(HERE)
+
+
+def reference_root():
+    """The reference checkout, or None (see the module docstring)."""
+    env = os.environ.get("MOMMS_REFERENCE_ROOT")
+    if env:
+        return env
+    sibling = os.path.join(os.path.dirname(REPO_ROOT), "reference")
+    return sibling if os.path.isdir(sibling) else None
+
+
 REF_KERNELS = [
     "ukernels/bli_gemm_haswell_asm_d6x8.c",
     "ukernels/bli_gemm_haswell_asm_d4x12.c",
@@ -48,11 +64,14 @@ def build_oracle(verbose=False):
     return ORACLE_SO
 
 
-def build_ref(verbose=False):
+def build_ref(verbose=False, root=None):
     """Compile the reference's own microkernels; returns the path or None."""
     if platform.machine() not in ("x86_64", "AMD64"):
         return None
-    srcs = [os.path.join(REF_ROOT, s) for s in REF_KERNELS]
+    root = root or reference_root()
+    if not root:
+        return None
+    srcs = [os.path.join(root, s) for s in REF_KERNELS]
     if not all(os.path.exists(s) for s in srcs):
         return None
     if _newer(REF_SO, srcs + [__file__]):
@@ -68,6 +87,10 @@ def build_ref(verbose=False):
 
 
 if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=None, help="reference checkout (default: see module docstring)")
+    args = ap.parse_args()
     print(build_oracle(verbose=True))
-    print(build_ref(verbose=True))
+    print(build_ref(verbose=True, root=args.reference))
     sys.exit(0)

@@ -130,3 +130,15 @@ def test_packed_operand_handles_checked_without_a_gpu(lib):
     assert lib.momms_gemm_validate(ctypes.byref(d2)) == mg.ERR_INVALID_ARG
     assert lib.momms_packed_destroy(ctypes.c_void_p(ctypes.addressof(buf))) == mg.ERR_INVALID_ARG
     assert lib.momms_packed_bytes(ctypes.c_void_p(ctypes.addressof(buf))) == 0
+
+
+def test_fault_injection_counters_without_a_gpu(lib):
+    """The injection hook is plain host state: set, read back, cleared."""
+    assert lib.momms_fault_inject(mg.FAULT_ALLOC, 3) == mg.OK
+    assert lib.momms_fault_pending(mg.FAULT_ALLOC) == 3
+    assert lib.momms_fault_pending(mg.FAULT_CUDA) == 0
+    assert lib.momms_fault_inject(mg.FAULT_ALLOC, 0) == mg.OK
+    assert lib.momms_fault_pending(mg.FAULT_ALLOC) == 0
+    assert lib.momms_fault_inject(9, 1) == mg.ERR_INVALID_ARG
+    assert lib.momms_fault_inject(mg.FAULT_CUDA, -1) == mg.ERR_INVALID_ARG
+    assert lib.momms_fault_pending(9) == -1

@@ -5,8 +5,10 @@ whose GPU memory already belongs to its own pool or framework, or a
 latency-critical loop that cannot afford cudaMalloc / cudaFree (their cost,
 their implicit synchronisation, or an out-of-memory failure midway). Its
 split-k scratch is a fixed device-global array shared by every call, so each
-case below runs two calls in a row and compares both with the ordinary
-momms_dgemm, within the componentwise bound the other GPU tests use.
+case below runs two calls in a row. The entry point runs the same kernel with
+the same tile / split-k plan as momms_dgemm, so both calls must equal
+momms_dgemm bit for bit, and each must also meet the componentwise bound
+against the double-double oracle directly.
 
 The file name makes pytest collect it last: a run that stops at the first
 failure has run every other test before this one.
@@ -51,14 +53,41 @@ def test_noalloc_matches_dgemm_twice(gpu, shape):
     torch.cuda.synchronize()
     C_ref = ref_t.cpu().numpy()
 
-    _, mag = ou.dd_gemm(A, B, C0)
-    tol = 2.0 * (k + 2) * U64 * mag
+    exact, mag = ou.dd_gemm(A, B, C0)
     for _ in range(2):  # two calls in a row: the shared scratch must not leak state
         C_t, _, _ = gu.to_device(C0)
         mg.check(_call(gpu.momms_dgemm_noalloc, A_t, B_t, C_t, m, n, k, 1.0, 1.0), gpu)
         torch.cuda.synchronize()
         C = C_t.cpu().numpy()
-        assert np.all(np.abs(C - C_ref) <= tol)
+        assert np.array_equal(C, C_ref)  # same kernel, same plan: same bits
+        assert ou.bound_ratio(C, exact, mag, k, U64) <= 1.0
+    bits = ctypes.c_uint32(0)
+    assert gpu.momms_noalloc_status(ctypes.byref(bits)) == mg.OK and bits.value == 0
+
+
+def test_noalloc_rejects_a_plan_larger_than_its_scratch(gpu):
+    """A split-k plan that needs more partial tiles than the fixed array holds
+    is refused before anything runs, and C is left as it was. The model never
+    plans more than one partial tile per SM; a tuning-table entry can."""
+    import torch
+    m, n, k = 1024, 1024, 4096  # 64 output tiles; 32 splits -> 2048 partial tiles
+    rng = np.random.default_rng(404)
+    A = np.asfortranarray(rng.uniform(-1, 1, (m, k)))
+    B = np.asfortranarray(rng.uniform(-1, 1, (k, n)))
+    C0 = np.asfortranarray(rng.uniform(-1, 1, (m, n)))
+    A_t, _, _ = gu.to_device(A)
+    B_t, _, _ = gu.to_device(B)
+    C_t, _, _ = gu.to_device(C0)
+    gpu.momms_tune_clear()
+    mg.check(gpu.momms_tune_import(f"0 0 {m} {n} {k} 32".encode()), gpu)
+    try:
+        rc = _call(gpu.momms_dgemm_noalloc, A_t, B_t, C_t, m, n, k, 1.0, 1.0)
+        torch.cuda.synchronize()
+        assert rc == mg.ERR_INVALID_ARG
+        assert b"no-alloc scratch" in gpu.momms_last_error()
+        assert np.array_equal(C_t.cpu().numpy(), C0)
+    finally:
+        gpu.momms_tune_clear()
 
 
 def test_noalloc_rejects_what_it_cannot_do_without_allocating(gpu):
