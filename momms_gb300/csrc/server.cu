@@ -204,6 +204,10 @@ struct Server {
           if (e == cudaSuccess) e = cudaEventRecord(b.ev, s);
           if (e != cudaSuccess) rc = cuda_fail(e, "batch event");
         }
+        // A batch that failed after some of its work was enqueued is finished
+        // only when that work is: its requests' outputs are not touched again
+        // once they are reported.
+        if (rc) cudaStreamSynchronize(s);
         lk.lock();
         launching -= 1;
         if (rc) {
