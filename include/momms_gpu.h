@@ -51,7 +51,10 @@ typedef enum {
   MOMMS_ERR_DEVICE_TIMEOUT = 6, /* a kernel's bounded wait expired */
   MOMMS_ERR_ADMISSION = 7,      /* serving: request larger than the budget */
   MOMMS_ERR_BUSY = 8,           /* serving: queue full or not ready */
-  MOMMS_ERR_SHUTDOWN = 9        /* serving: server stopped */
+  MOMMS_ERR_SHUTDOWN = 9,       /* serving: server stopped */
+  MOMMS_ERR_TARGET_UNREACHABLE = 10 /* OZAKI with an automatic slice count: 15 slices (the most) cannot
+                                       guarantee the requested error for every entry; C holds the 15-slice
+                                       result and momms_last_info's bound_rel_err the bound that holds */
 } momms_status;
 
 typedef enum { MOMMS_DTYPE_F64 = 0, MOMMS_DTYPE_F32 = 1 } momms_dtype;
@@ -83,8 +86,9 @@ typedef struct {
   int64_t m, n, k;
   double alpha, beta; /* used in the operands' dtype */
   momms_operand a, b, c;
-  double target_rel_err; /* OZAKI: requested max |dC_ij| / (|A||B|)_ij; 0 = FP64 level */
-  int32_t slices;        /* OZAKI: slice count, 0 = chosen from target_rel_err */
+  double target_rel_err; /* OZAKI: requested max |dC_ij| / (|A||B|)_ij; 0 = FP64 level (2^-52) */
+  int32_t slices;        /* OZAKI: slice count 1..15 (8 bits each), 0 = chosen from target_rel_err so
+                            that a rigorous bound holds for every entry (see momms_last_info) */
   int32_t flags;         /* reserved, must be 0 */
 } momms_gemm_desc;
 
@@ -154,7 +158,7 @@ int momms_noalloc_status(uint32_t* bits);
  *
  * role: MOMMS_ROLE_A (rows x cols = m x k) or MOMMS_ROLE_B (k x n); the pack
  * fits only that position and those sizes. src: host or device view (AUTO /
- * HOST / DEVICE). slices: OZAKI only, 1..16 (0 = 7 slices of 8 bits, the
+ * HOST / DEVICE). slices: OZAKI only, 1..15 (0 = 7 slices of 8 bits, the
  * count the FP64-level target takes for operands without a wide exponent
  * spread). Emulated calls with k > 32704 cannot use packed operands (their k
  * slabs re-scale per slab).
@@ -293,7 +297,8 @@ typedef struct {
   int32_t splits;         /* plain paths: k splits */
   int32_t slice_variant;  /* tensor-core paths: slice kernel variant run: 0 = one CTA per tile,
                              2 = CTA pairs with one cta_group::2 MMA (1 is unused) */
-  double bound_rel_err;   /* OZAKI: predicted worst-case |dC|/(|A||B|) */
+  double bound_rel_err;   /* OZAKI with an automatic slice count: a rigorous bound on
+                             max_ij |dC_ij| / (|A||B|)_ij of the product, over every entry (-1 otherwise) */
 } momms_call_info;
 int momms_last_info(momms_call_info* out);
 
@@ -354,7 +359,8 @@ typedef enum {
   MOMMS_KERNEL_SLICE_TF32 = 3,   /* tcgen05 slice products, split-TF32 f32 */
   MOMMS_KERNEL_PREP = 4,         /* exponent scan, slicing / splitting, repack */
   MOMMS_KERNEL_COMBINE = 5,      /* Ozaki FP64 recombination */
-  MOMMS_KERNEL_CLASSES = 6
+  MOMMS_KERNEL_BOUND = 6,        /* Ozaki: guaranteed error bound (bf16 magnitude product on tcgen05) */
+  MOMMS_KERNEL_CLASSES = 7
 } momms_kernel_class;
 int momms_timing_enable(int on);
 int momms_timing_read(int kernel_class, double* total_ms, unsigned long long* launches, int reset);

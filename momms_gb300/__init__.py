@@ -24,6 +24,7 @@ ERR_DEVICE_TIMEOUT = 6
 ERR_ADMISSION = 7
 ERR_BUSY = 8
 ERR_SHUTDOWN = 9
+ERR_TARGET_UNREACHABLE = 10
 
 KERNEL_DGEMM_DMMA = 0
 KERNEL_SGEMM_FFMA = 1
@@ -31,6 +32,7 @@ KERNEL_SLICE_OZAKI = 2
 KERNEL_SLICE_TF32 = 3
 KERNEL_PREP = 4
 KERNEL_COMBINE = 5
+KERNEL_BOUND = 6
 
 FAULT_ALLOC = 0
 FAULT_CUDA = 1

@@ -103,16 +103,18 @@ DeviceState* device_state() {
     }
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    cudaStream_t cs = nullptr, cs2 = nullptr, aux = nullptr;
+    cudaStream_t cs = nullptr, cs2 = nullptr, aux = nullptr, aux2 = nullptr;
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) != cudaSuccess) {
+        (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&aux2, cudaStreamNonBlocking)) != cudaSuccess) {
       cuda_fail(e, "library stream");
       return nullptr;
     }
     d.copy_stream = cs;
     d.copy_stream2 = cs2;
     d.aux = aux;
+    d.aux2 = aux2;
     d.pool = pool;
     d.sm_count = sms;
     d.status = st;
@@ -209,7 +211,7 @@ int validate(const momms_gemm_desc* d) {
     return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki emulation is an f64 mode");
   if (d->precision == MOMMS_PREC_SPLIT_TF32 && d->dtype != MOMMS_DTYPE_F32)
     return fail(MOMMS_ERR_UNSUPPORTED, "split-TF32 is an f32 mode");
-  if (d->precision == MOMMS_PREC_OZAKI && (d->slices < 0 || d->slices > 16))
+  if (d->precision == MOMMS_PREC_OZAKI && (d->slices < 0 || d->slices > kOzakiMaxSlices))
     return fail(MOMMS_ERR_INVALID_ARG, "Ozaki slice count %d outside 0..16", d->slices);
   if (d->precision == MOMMS_PREC_OZAKI && !(d->target_rel_err >= 0.0 && d->target_rel_err < 1.0))
     return fail(MOMMS_ERR_INVALID_ARG, "target_rel_err must be in [0, 1)");
@@ -326,7 +328,7 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
       BlockPlan plan;
       rc = plan_blocks(*d, host, budget, &plan);
       if (!rc) rc = gemm_streamed(*d, host, plan, s);
-      if (!rc) g_last_info = g_info;
+      if (!rc || rc == MOMMS_ERR_TARGET_UNREACHABLE) g_last_info = g_info;
       return rc;
     }
   }
@@ -400,7 +402,14 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
       if (need[i]) rc = stage_copy_in(*ops[i], es, st[i], s);
   }
 
+  // an unreachable accuracy target still leaves a result in C: finish the
+  // call (C's copy-back included) and report it at the end
+  int verdict = MOMMS_OK;
   if (!rc) rc = dispatch(g, d, s);
+  if (rc == MOMMS_ERR_TARGET_UNREACHABLE) {
+    verdict = rc;
+    rc = MOMMS_OK;
+  }
   if (!rc && host[2]) {
     if (sc.hooks.writeback) rc = columns_done(g, sc.hooks.written, g.n, s);  // what the path left
     else rc = stage_out(*ops[2], es, st[2], s);
@@ -421,7 +430,10 @@ int gemm_impl(const momms_gemm_desc* d, cudaStream_t s) {
   }
   for (int i = 0; i < 6; ++i)
     if (sc.ev[i]) cudaEventDestroy(sc.ev[i]);
-  if (!rc) g_last_info = g_info;
+  if (!rc) {
+    g_last_info = g_info;
+    rc = verdict;
+  }
   return rc;
 }
 
@@ -514,6 +526,7 @@ const char* momms_status_string(int status) {
     case MOMMS_ERR_ADMISSION: return "request exceeds the admission budget";
     case MOMMS_ERR_BUSY: return "busy";
     case MOMMS_ERR_SHUTDOWN: return "server stopped";
+    case MOMMS_ERR_TARGET_UNREACHABLE: return "requested accuracy cannot be guaranteed with 15 slices";
     default: return "unknown status";
   }
 }

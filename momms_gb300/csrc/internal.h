@@ -19,6 +19,7 @@ struct DeviceState {
   cudaStream_t copy_stream = nullptr;   // host->device staging copies of momms_gemm calls
   cudaStream_t copy_stream2 = nullptr;  // device->host copies (streamed calls, C write-back)
   cudaStream_t aux = nullptr;           // second compute stream of column-chunked emulated calls
+  cudaStream_t aux2 = nullptr;          // emulated calls: the guaranteed bound and, under it, recombinations
 };
 
 // Stream-ordered scratch allocation (free with cudaFreeAsync) from the
@@ -212,6 +213,10 @@ int launch_sgemm_tf32x3(const DevGemm& g, cudaStream_t s);
 // Longest k of one emulated launch (8-bit digits: 511 k-blocks of 64 keep a
 // digit pair's int32 sum exact); longer k runs in slabs accumulated into C.
 constexpr int64_t kOzakiMaxK = 32704;
+// Most slices of an emulated call: 15 digits of 8 bits (120 bits). The digit
+// extraction works in 128-bit integers and the top digit of an s-slice split
+// needs 8 * (s - 1) + 9 bits, so 16 slices would not fit.
+constexpr int kOzakiMaxSlices = 15;
 // Ozaki FP64 emulation: target relative error (0 = FP64 level) and slice count
 // (0 = chosen from the target). *slices_used receives the count actually used.
 int launch_dgemm_ozaki(const DevGemm& g, double target_rel_err, int slices, int* slices_used, cudaStream_t s);

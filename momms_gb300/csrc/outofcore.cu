@@ -219,6 +219,7 @@ int gemm_streamed(const momms_gemm_desc& d, const bool host[3], const BlockPlan&
   const momms_operand* ops[3] = {&d.a, &d.b, &d.c};
   Slots slots[3];
   int rc = MOMMS_OK;
+  int verdict = MOMMS_OK;  // MOMMS_ERR_TARGET_UNREACHABLE from any block
   cudaError_t e = cudaSuccess;
   cudaEvent_t ev_alloc = nullptr, ev_cols = nullptr, ev_end[2] = {nullptr, nullptr};
 
@@ -366,6 +367,10 @@ int gemm_streamed(const momms_gemm_desc& d, const bool host[3], const BlockPlan&
     bd.k = g.k;
     bd.beta = g.beta;
     rc = run_device_gemm(g, bd, s);
+    if (rc == MOMMS_ERR_TARGET_UNREACHABLE) {  // the block holds a result; report after the rest
+      verdict = rc;
+      rc = MOMMS_OK;
+    }
     if (rc) break;
     for (int x = 0; x < 2; ++x)
       if (host[x]) {
@@ -414,7 +419,7 @@ int gemm_streamed(const momms_gemm_desc& d, const bool host[3], const BlockPlan&
     }
   for (cudaEvent_t ev : {ev_alloc, ev_cols, ev_end[0], ev_end[1]})
     if (ev) cudaEventDestroy(ev);
-  return rc;
+  return rc ? rc : verdict;
 }
 
 }  // namespace momms

@@ -200,7 +200,7 @@ void launch_ozaki_planes(const double* x, int64_t sr, int64_t sp, int64_t R, int
   planes::launch_to_planes(x, sr, sp, R, K, planes, ldp, plane_elems, OzakiSliceOp<NS>{exps}, s);
 }
 
-// Runtime slice count -> the unrolled kernel for it (1..16).
+// Runtime slice count -> the unrolled kernel for it (1..kOzakiMaxSlices).
 void ozaki_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, __half* planes, int64_t ldp,
                   int64_t plane_elems, const int* exps, cudaStream_t s) {
   switch (ns) {
@@ -208,7 +208,7 @@ void ozaki_planes(int ns, const double* x, int64_t sr, int64_t sp, int64_t R, in
   case N: launch_ozaki_planes<N>(x, sr, sp, R, K, planes, ldp, plane_elems, exps, s); break;
     MOMMS_OZAKI_NS(1) MOMMS_OZAKI_NS(2) MOMMS_OZAKI_NS(3) MOMMS_OZAKI_NS(4) MOMMS_OZAKI_NS(5) MOMMS_OZAKI_NS(6)
     MOMMS_OZAKI_NS(7) MOMMS_OZAKI_NS(8) MOMMS_OZAKI_NS(9) MOMMS_OZAKI_NS(10) MOMMS_OZAKI_NS(11) MOMMS_OZAKI_NS(12)
-    MOMMS_OZAKI_NS(13) MOMMS_OZAKI_NS(14) MOMMS_OZAKI_NS(15) MOMMS_OZAKI_NS(16)
+    MOMMS_OZAKI_NS(13) MOMMS_OZAKI_NS(14) MOMMS_OZAKI_NS(15)
 #undef MOMMS_OZAKI_NS
     default: break;
   }
@@ -544,7 +544,7 @@ int choose_slices(const DevGemm& g, const int* rexp, const int* cexp, double tar
   if (!(q1 > 0.0)) q1 = 4.0;  // no usable sample (zero operands): nominal uniform-data value
   if (!(q2 > 0.0)) q2 = 4.0;
   int ns = 1;
-  while (ns < 16 && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
+  while (ns < kOzakiMaxSlices && ozaki_bound(ns, bits, q1, q2) > tgt) ++ns;
   *ns_out = ns;
   if (bound_out) *bound_out = ozaki_bound(ns, bits, q1, q2);
   return MOMMS_OK;
@@ -576,35 +576,8 @@ void ozaki_operand_planes(int ns, const double* x, int64_t sr, int64_t sp, int64
 
 int set_attrs_ozaki() {
   cudaError_t e = sp::set_slice_attrs<0, sp::EPI_OZAKI>();
+  if (e == cudaSuccess) e = sp::set_slice_attrs<2, sp::EPI_BOUND>();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(Ozaki)");
-}
-
-int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
-  // a packed operand fixes the count
-  const PackedOperand* pa = packed_of(d.a);
-  const PackedOperand* pb = packed_of(d.b);
-  if (pa || pb) {
-    *slices = (pa ? pa : pb)->np;
-    return MOMMS_OK;
-  }
-  DevGemm g;
-  g.dtype = d.dtype;
-  g.m = d.m; g.n = d.n; g.k = d.k;
-  g.alpha = d.alpha; g.beta = d.beta;
-  g.a = DevMat{d.a.ptr, d.a.rs, d.a.cs};
-  g.b = DevMat{d.b.ptr, d.b.rs, d.b.cs};
-  g.c = DevMat{d.c.ptr, d.c.rs, d.c.cs};
-  void* ebuf = nullptr;
-  cudaError_t ce = scratch_alloc(&ebuf, (size_t)(g.m + g.n) * (sizeof(unsigned long long) + sizeof(int)), s);
-  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
-  unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
-  int* exps = reinterpret_cast<int*>(maxbits + (g.m + g.n));
-  int rc = compute_exponents(g, maxbits, exps, s);
-  if (!rc) rc = choose_slices(g, exps, exps + g.m, d.target_rel_err, kDigitBits, s, slices, nullptr);
-  cudaFreeAsync(ebuf, s);
-  cudaError_t e2 = cudaStreamSynchronize(s);
-  if (!rc && e2 != cudaSuccess) rc = cuda_fail(e2, "stream synchronize");
-  return rc;
 }
 
 namespace {
@@ -707,6 +680,283 @@ void column_cuts(int64_t n, int nch, bool deferred, int64_t* cut) {
 }
 }  // namespace
 
+namespace {
+
+// ---- The guaranteed bound -------------------------------------------------
+// Rigorous componentwise bound of an s-slice product relative to |A||B|, from
+// the maxima q1 = max (sum|a_i.| 2^-e_i + sum|b_.j| 2^-f_j) / L_ij and
+// q2 = max k / L_ij (L_ij <= (|A||B|)_ij 2^-(e_i+f_j)): digit rounding of A and
+// B costs 2^(-8s-1) (q1 + 2^(-8s-1) q2), and the diagonals beyond s+1 that the
+// triangular scheme drops (pairs of centred digits, |d| <= 2^7) at most
+// 2^(-8s-1) (s-1)/2 (256/255) q2.
+double guaranteed_bound(int s, double q1, double q2) {
+  const double u = ldexp(1.0, -kDigitBits * s - 1);
+  return u * (q1 + (0.5 * (s - 1) * (256.0 / 255.0) + u) * q2);
+}
+double target_or_fp64(double target) { return target > 0.0 ? target : ldexp(1.0, -52); }
+// Smallest slice count (at most kOzakiMaxSlices) whose guaranteed bound
+// meets the target; *reachable is false if the most slices do not, or if some
+// entry is uncovered.
+int guaranteed_slices(double target, double q1, double q2, bool uncovered, bool* reachable) {
+  const double tgt = target_or_fp64(target);
+  int ns = 1;
+  while (ns < kOzakiMaxSlices && guaranteed_bound(ns, q1, q2) > tgt) ++ns;
+  *reachable = !uncovered && guaranteed_bound(ns, q1, q2) <= tgt;
+  return uncovered ? kOzakiMaxSlices : ns;
+}
+
+// Scratch of the bound: bf16 magnitude planes of A (m rows) and of B
+// transposed (n rows), K-major with row stride kp; the rows' sums of scaled
+// magnitudes (units of 2^-40, m then n, contiguous) and the result words
+// right after them: out[0], out[1] the maxima (float bits), out[2..3] a
+// 64-bit count of covered entries.
+struct BoundWork {
+  uint16_t* mag_a;
+  uint16_t* mag_b;
+  unsigned long long* sum_a;
+  unsigned long long* sum_b;
+  unsigned* out;
+  int64_t kp;
+};
+size_t bound_work_bytes(int64_t m, int64_t n, int64_t k) {
+  const int64_t kp = round_up(k, 8);
+  return (size_t)round_up(m * kp * 2, 256) + (size_t)round_up(n * kp * 2, 256) + (size_t)(m + n) * 8 + 16;
+}
+void bound_work_carve(void* base, int64_t m, int64_t n, int64_t k, BoundWork* w) {
+  char* p = static_cast<char*>(base);
+  w->kp = round_up(k, 8);
+  w->mag_a = reinterpret_cast<uint16_t*>(p);
+  p += round_up(m * w->kp * 2, 256);
+  w->mag_b = reinterpret_cast<uint16_t*>(p);
+  p += round_up(n * w->kp * 2, 256);
+  w->sum_a = reinterpret_cast<unsigned long long*>(p);
+  w->sum_b = w->sum_a + m;
+  w->out = reinterpret_cast<unsigned*>(w->sum_b + n);
+}
+
+// |v| 2^-e for the bound: as bf16 rounded toward zero (0 below bf16's normal
+// range: the lower bound only loses that term), and as ceil(|v| 2^(40 - e)),
+// an upward-rounded fixed-point term of the row sum. Integer arithmetic on
+// the bit pattern only. Rows holding a NaN or an infinity (e == INT32_MAX)
+// give 0: their results are NaN and need no bound. With `indicator`, *bf is
+// 1.0 for every element that is nonzero (in a finite row), else 0.
+__device__ __forceinline__ void magnitude(double v, int e, bool indicator, uint16_t* bf, unsigned long long* fix) {
+  *bf = 0;
+  *fix = 0;
+  const unsigned long long ab = abs_bits(v);
+  if (ab == 0 || e == INT32_MAX || ab >= 0x7ff0000000000000ull) return;
+  if (indicator) {
+    *bf = 0x3f80;  // 1.0
+    return;
+  }
+  const int be = (int)(ab >> 52);
+  const unsigned long long M = be ? ((ab & ((1ull << 52) - 1)) | (1ull << 52)) : ab;
+  const int E = be ? be - 1075 : -1074;           // |v| = M 2^E
+  const int nb = 64 - __clzll((long long)M);      // significant bits of M
+  const int X = E - e + nb - 1;                   // |v| 2^-e in [2^X, 2^(X+1)), X <= -1
+  if (X + 127 >= 1) {
+    const unsigned top = (unsigned)(nb >= 8 ? (M >> (nb - 8)) : (M << (8 - nb)));  // leading 8 bits
+    *bf = (uint16_t)(((unsigned)(X + 127) << 7) | (top & 0x7fu));
+  }
+  const int sh = E - e + 40;  // |v| 2^(40-e) = M 2^sh < 2^40
+  if (sh >= 0) *fix = M << sh;
+  else if (sh > -64) *fix = (M >> (-sh)) + ((M & ((1ull << (-sh)) - 1)) ? 1ull : 0ull);
+  else *fix = 1ull;
+}
+
+// Magnitude plane and row sums of an R x K view (element (r, p) at
+// x[r*sr + p*sp]) under the row exponents: a block stages 32 rows x 64 of p
+// (coalesced along whichever index is contiguous), then each warp converts
+// one row's 64 elements (a lane per pair), sums the fixed-point terms over the
+// warp and posts one 64-bit atomicAdd (exact, so the sums do not depend on
+// timing). With `indicator` it writes the 0/1 plane of nonzero elements and
+// no sums.
+__global__ void __launch_bounds__(256) magnitude_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
+                                                        int64_t R, int64_t K, bool r_contig,
+                                                        const int* __restrict__ exps, uint16_t* __restrict__ plane,
+                                                        int64_t ldp, unsigned long long* __restrict__ sums,
+                                                        bool indicator) {
+  constexpr int TR = 32, TP = 64;
+  __shared__ double tile[TR][TP + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t p0 = (int64_t)blockIdx.x * TP;
+  for (int64_t r0 = (int64_t)blockIdx.y * TR; r0 < R; r0 += (int64_t)gridDim.y * TR) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < TR * TP / 256; ++i) {
+      const int lin = tid + 256 * i;
+      const int rl = r_contig ? (lin % TR) : (lin / TP);
+      const int pl = r_contig ? (lin / TR) : (lin % TP);
+      const int64_t r = r0 + rl, pp = p0 + pl;
+      tile[rl][pl] = (r < R && pp < K) ? x[r * sr + pp * sp] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int rl = warp; rl < TR; rl += 8) {
+      const int64_t r = r0 + rl;
+      if (r >= R) break;  // uniform over the warp
+      const int e = exps[r];
+      const int64_t pp = p0 + 2 * lane;
+      uint16_t b0 = 0, b1 = 0;
+      unsigned long long f0 = 0, f1 = 0;
+      if (pp < K) {
+        magnitude(tile[rl][2 * lane], e, indicator, &b0, &f0);
+        magnitude(tile[rl][2 * lane + 1], e, indicator, &b1, &f1);  // beyond K: the tile holds 0
+        *reinterpret_cast<unsigned*>(plane + r * ldp + pp) = (unsigned)b0 | ((unsigned)b1 << 16);
+      }
+      if (!indicator) {
+        unsigned long long t = f0 + f1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0 && t) atomicAdd(&sums[r], t);
+      }
+    }
+  }
+}
+
+int enqueue_magnitudes(const double* x, int64_t sr, int64_t sp, int64_t R, int64_t K, const int* exps,
+                       uint16_t* plane, int64_t kp, unsigned long long* sums, cudaStream_t s, bool indicator = false) {
+  if (R == 0) return MOMMS_OK;
+  const bool r_contig = (sr == 1 && sp != 1);
+  dim3 grid((unsigned)ceil_div(K, 64), (unsigned)std::min<int64_t>(ceil_div(R, 32), 65535));
+  {
+    KernelTimer kt(MOMMS_KERNEL_PREP, s);
+    magnitude_kernel<<<grid, 256, 0, s>>>(x, sr, sp, R, K, r_contig, exps, plane, kp, sums, indicator);
+  }
+  note_launch();
+  const cudaError_t e = launch_status();
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "Ozaki bound magnitudes");
+}
+
+// The bound kernel (bf16 magnitude product on tcgen05, EPI_BOUND) over all of
+// C; the maxima land in w.out[0..1].
+int enqueue_bound_kernel(const BoundWork& w, int64_t m, int64_t n, int64_t k, bool count_only, unsigned* status,
+                         int sm_count, cudaStream_t s) {
+  CUtensorMap tmA, tmB, tmB_half;
+  uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, 1};
+  uint64_t strides[2] = {(uint64_t)w.kp * 2, (uint64_t)m * w.kp * 2};
+  uint32_t box[3] = {64, (uint32_t)sp::BM, 1};
+  int rc = encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, w.mag_a, dims, strides, box,
+                        CU_TENSOR_MAP_SWIZZLE_128B);
+  if (rc) return rc;
+  uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)n, 1};
+  uint64_t stridesb[2] = {(uint64_t)w.kp * 2, (uint64_t)n * w.kp * 2};
+  uint32_t boxb[3] = {64, (uint32_t)sp::BN, 1};
+  rc = encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, w.mag_b, dimsb, stridesb, boxb,
+                    CU_TENSOR_MAP_SWIZZLE_128B);
+  if (rc) return rc;
+  uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};
+  rc = encode_tiled(&tmB_half, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, w.mag_b, dimsb, stridesb, boxh,
+                    CU_TENSOR_MAP_SWIZZLE_128B);
+  if (rc) return rc;
+  sp::Params p;
+  memset(&p, 0, sizeof(p));
+  p.m = m;
+  p.n = n;
+  p.kelems = 64;
+  p.kblocks = (int)ceil_div(k, 64);
+  p.tiles_m = (int)ceil_div(m, sp::BM);
+  p.tiles_n = (int)ceil_div(n, sp::BN);
+  p.ngroups = 1;
+  p.group_begin[0] = 0;
+  p.group_begin[1] = 1;
+  p.pair_a[0] = 0;
+  p.pair_b[0] = 0;
+  p.pair_w[0] = 1;
+  p.chunk_cap = std::max(1, p.kblocks);  // one FP32 accumulation over all of k
+  p.merge_pairs = 0;
+  p.msum_a = w.sum_a;
+  p.msum_b = w.sum_b;
+  // The FP32 sum of non-negative exact bf16 products, accumulated by the
+  // tensor core (alignment and truncation at most a few units of 2^-24 per
+  // step), is taken to lose at most max(k, 64) 2^-21 of itself.
+  const double lbs = 1.0 - (double)std::max<int64_t>(k, 64) * ldexp(1.0, -21);
+  p.lb_scale = (float)lbs;
+  if ((double)p.lb_scale > lbs) p.lb_scale = nextafterf(p.lb_scale, 0.0f);  // rounded down
+  p.kf = (float)k;
+  p.bound_out = w.out;
+  p.bound_count = reinterpret_cast<unsigned long long*>(w.out + 2);
+  p.count_only = count_only ? 1 : 0;
+  p.status = status;
+  cudaError_t ce;
+  {
+    KernelTimer kt(MOMMS_KERNEL_BOUND, s);
+    int variant = 0;
+    ce = sp::launch_slice<2, sp::EPI_BOUND>(tmA, tmB, tmB_half, p, sm_count, s, &variant);
+    if (ce == cudaSuccess) ce = launch_status();
+  }
+  note_launch();
+  return ce == cudaSuccess ? MOMMS_OK : cuda_fail(ce, "Ozaki bound launch");
+}
+
+// The bound's result, once the bound kernel is enqueued on `s`: the two
+// maxima, and whether some entry is uncovered. The kernel counts the entries
+// with a positive lower bound; if that is not all of C, a second pass over
+// 0/1 indicator planes counts the entries with any nonzero product term. An
+// entry counted there but not by the bound has every term below FP32's range
+// (relative to 2^(e_i+f_j)): no slice count can vouch for it. Entries with no
+// nonzero term are exact (their digits are all zero). Synchronises `s`.
+struct OperandViews {
+  const double* a;
+  int64_t a_rs, a_cs;
+  const double* b;
+  int64_t b_rs, b_cs;
+  const int* rexp;
+  const int* cexp;
+};
+int bound_result(const BoundWork& w, const OperandViews& v, int64_t m, int64_t n, int64_t k, DeviceState* ds,
+                 cudaStream_t s, float* q1, float* q2, bool* uncovered) {
+  unsigned words[4] = {0, 0, 0, 0};
+  cudaError_t ce = cudaMemcpyAsync(words, w.out, sizeof(words), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound");
+  memcpy(q1, &words[0], 4);
+  memcpy(q2, &words[1], 4);
+  unsigned long long covered;
+  memcpy(&covered, &words[2], 8);
+  *uncovered = false;
+  if (covered >= (unsigned long long)m * (unsigned long long)n) return MOMMS_OK;
+  // indicator pass (sparse operands, or terms beyond FP32's range)
+  ce = cudaMemsetAsync(w.out + 2, 0, 8, s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound");
+  int rc = enqueue_magnitudes(v.a, v.a_rs, v.a_cs, m, k, v.rexp, w.mag_a, w.kp, nullptr, s, true);
+  if (!rc) rc = enqueue_magnitudes(v.b, v.b_cs, v.b_rs, n, k, v.cexp, w.mag_b, w.kp, nullptr, s, true);
+  if (!rc) rc = enqueue_bound_kernel(w, m, n, k, true, ds->status, ds->sm_count, s);
+  if (rc) return rc;
+  unsigned long long nonzero = 0;
+  ce = cudaMemcpyAsync(&nonzero, w.out + 2, 8, cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound");
+  *uncovered = nonzero > covered;
+  return MOMMS_OK;
+}
+
+// Events of one emulated call's streams.
+struct Events {
+  cudaEvent_t fork = nullptr, join = nullptr, join2 = nullptr, bound = nullptr;
+  cudaEvent_t mag[kMaxChunks] = {}, prod[kMaxChunks] = {};
+  int create(int nch) {
+    cudaError_t e = cudaSuccess;
+    for (cudaEvent_t* p : {&fork, &join, &join2, &bound})
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(p, cudaEventDisableTiming);
+    for (int c = 0; c < nch && e == cudaSuccess; ++c) {
+      e = cudaEventCreateWithFlags(&mag[c], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&prod[c], cudaEventDisableTiming);
+    }
+    return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "Ozaki chunk events");
+  }
+  void destroy() {
+    for (cudaEvent_t* p : {&fork, &join, &join2, &bound})
+      if (*p) cudaEventDestroy(*p);
+    for (int c = 0; c < kMaxChunks; ++c) {
+      if (mag[c]) cudaEventDestroy(mag[c]);
+      if (prod[c]) cudaEventDestroy(prod[c]);
+    }
+  }
+};
+
+}  // namespace
+
 int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
@@ -718,6 +968,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     // accumulating into C with beta = 1 like the reference's PartK
     // (src/composables/part.rs:96-110); each slab meets the target on its own
     const int64_t nslab = ceil_div(g.k, kMaxK), kb = round_up(ceil_div(g.k, nslab), 64);
+    bool unreachable = false;
     // deferred B / C arrive whole before the first slab
     for (int w = 1; w <= 2 && g.staging; ++w)
       if (g.staging->deferred[w]) {
@@ -739,9 +990,10 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
         gs.staging->writeback = nullptr;  // C goes back after the last slab
       }
       int rc = launch_dgemm_ozaki(gs, target, slices, slices_used, s);
-      if (rc) return rc;
+      if (rc == MOMMS_ERR_TARGET_UNREACHABLE) unreachable = true;
+      else if (rc) return rc;
     }
-    return MOMMS_OK;
+    return unreachable ? MOMMS_ERR_TARGET_UNREACHABLE : MOMMS_OK;
   }
   const int bits = kDigitBits;
   const int64_t m = g.m, n = g.n, k = g.k;
@@ -820,19 +1072,63 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   const int* cexp = PB ? PB->exps : cexp_w;
 
   int ns = ns_fixed ? ns_fixed : slices;
-  if (ns <= 0) {
+  // Automatic count, guaranteed for every entry by the bound kernel (the
+  // bf16 magnitude product, about 1/28 of the slice products' tensor work):
+  //  * operands on the device (B not deferred): the bound runs first and the
+  //    count comes from it (one synchronisation, as the choice always had);
+  //  * B arriving from host memory by column chunks: a sampled estimate
+  //    starts the work on A and the first chunks early, the bound follows once
+  //    all of B is in, and the recombinations (the only kernels writing C)
+  //    wait for its verdict; a count that misses the target is redone with the
+  //    bound's count while C still holds its input.
+  const bool automatic = ns <= 0;
+  const bool verify = automatic && defer_b;
+  bool b_exps_ready = false;
+  int verdict = MOMMS_OK;
+  BoundWork bw{};
+  void* bw_mem = nullptr;
+  if (automatic) {
+    if ((ce = scratch_alloc(&bw_mem, bound_work_bytes(m, n, k), s)) != cudaSuccess)
+      return cuda_fail(ce, "Ozaki bound scratch");
+    bound_work_carve(bw_mem, m, n, k, &bw);
+    // sums and result words start at zero (they are contiguous); A's
+    // magnitudes on s after A's exponents
+    ce = cudaMemsetAsync(bw.sum_a, 0, (size_t)(m + n) * sizeof(unsigned long long) + 4 * sizeof(unsigned), s);
+    rc = ce == cudaSuccess ? enqueue_magnitudes(A, g.a.rs, g.a.cs, m, k, rexp, bw.mag_a, bw.kp, bw.sum_a, s)
+                           : cuda_fail(ce, "Ozaki bound scratch");
+    if (rc) {
+      cudaFreeAsync(bw_mem, s);
+      return rc;
+    }
+  }
+  ScratchGuard free_bw(bw_mem, s);
+  if (automatic && !verify) {
+    // all of B's exponents and magnitudes, the bound, the count
+    if ((ce = wait_operand(g, 1, s)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+    rc = ozaki_operand_exponents(B, g.b.cs, g.b.rs, n, k, maxbits + m, cexp_w, s);
+    if (!rc) rc = enqueue_magnitudes(B, g.b.cs, g.b.rs, n, k, cexp_w, bw.mag_b, bw.kp, bw.sum_b, s);
+    if (!rc) rc = enqueue_bound_kernel(bw, m, n, k, false, ds->status, ds->sm_count, s);
+    float q1f = 0.0f, q2f = 0.0f;
+    bool uncovered = false;
+    if (!rc)
+      rc = bound_result(bw, OperandViews{A, g.a.rs, g.a.cs, B, g.b.rs, g.b.cs, rexp, cexp_w}, m, n, k, ds, s, &q1f,
+                        &q2f, &uncovered);
+    if (rc) return rc;
+    bool reachable = false;
+    ns = guaranteed_slices(target, q1f, q2f, uncovered, &reachable);
+    call_info().bound_rel_err = uncovered ? HUGE_VAL : guaranteed_bound(ns, q1f, q2f);
+    if (!reachable) verdict = MOMMS_ERR_TARGET_UNREACHABLE;
+    b_exps_ready = true;
+  } else if (automatic) {
     // B at the sampled columns, and their exponents
-    ce = defer_b ? cudaStreamWaitEvent(s, ev_sample, 0) : wait_operand(g, 1, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "operand staging");
+    if ((ce = cudaStreamWaitEvent(s, ev_sample, 0)) != cudaSuccess) return cuda_fail(ce, "operand staging");
     {
       KernelTimer kt(MOMMS_KERNEL_PREP, s);
       sample_col_exps_kernel<<<kSamples, 256, 0, s>>>(B, g.b.rs, g.b.cs, m, n, k, cexp_w);
     }
     note_launch();
-    double bound = 0.0;
-    rc = choose_slices(g, rexp, cexp_w, target, bits, s, &ns, &bound);
+    rc = choose_slices(g, rexp, cexp_w, target, bits, s, &ns, nullptr);
     if (rc) return rc;
-    call_info().bound_rel_err = bound;
   }
   if (slices_used) *slices_used = ns;
 
@@ -936,15 +1232,46 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.rsc = g.c.rs;
   cp.csc = g.c.cs;
 
-  // the second stream starts after everything above (scratch, A, the choice)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  if (nch > 1) {
-    ce = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
-    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
-    if (ce == cudaSuccess) ce = cudaEventRecord(ev_fork, s);
-    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ds->aux, ev_fork, 0);
-    if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+  // The second stream starts after everything above (scratch, A, the
+  // choice), and so does the verify stream V, which runs the bound kernel
+  // and, under verification, the recombinations.
+  cudaStream_t V = verify ? ds->aux2 : nullptr;
+  Events ev;
+  if (nch > 1 || verify) {
+    rc = ev.create(nch);
+    if (!rc) {
+      ce = cudaEventRecord(ev.fork, s);
+      if (ce == cudaSuccess && nch > 1) ce = cudaStreamWaitEvent(ds->aux, ev.fork, 0);
+      if (ce == cudaSuccess && verify) ce = cudaStreamWaitEvent(V, ev.fork, 0);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+    }
   }
+  // Recombination of chunk c (columns j0..j1 of C) on stream Y: with C staged
+  // from host memory and one chunk, in column ranges each copied back while
+  // the next is computed.
+  auto combine_chunk = [&](int c, cudaStream_t Y) -> int {
+    const int64_t j0 = cut[c], j1 = cut[c + 1], w = j1 - j0;
+    cudaError_t e = defer_c ? cudaStreamWaitEvent(Y, ev_c[c], 0) : wait_operand(g, 2, Y);
+    if (e != cudaSuccess) return cuda_fail(e, "operand staging");
+    const int64_t nsub = (nch == 1 && stg && stg->writeback) ? std::min<int64_t>(4, w) : 1;
+    for (int64_t q = 0; q < nsub; ++q) {
+      cp.j0 = j0 + w * q / nsub;
+      cp.j1 = j0 + w * (q + 1) / nsub;
+      const int64_t bx = ceil_div(m, 512);
+      const int64_t by =
+          std::min<int64_t>({cp.j1 - cp.j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
+      {
+        KernelTimer kt(MOMMS_KERNEL_COMBINE, Y);
+        combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, Y>>>(cp);
+      }
+      note_launch();
+      e = launch_status();
+      if (e != cudaSuccess) return cuda_fail(e, "Ozaki launch");
+      const int r2 = columns_done(g, cp.j0, cp.j1, Y);
+      if (r2) return r2;
+    }
+    return MOMMS_OK;
+  };
   for (int c = 0; c < nch && !rc; ++c) {
     const int64_t j0 = cut[c], j1 = cut[c + 1], w = j1 - j0;
     if (w <= 0) continue;
@@ -957,12 +1284,21 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     }
     const double* Bc = B + j0 * g.b.cs;
     if (!PB) {
-      rc = ozaki_operand_exponents(Bc, g.b.cs, g.b.rs, w, k, maxbits + m + j0, cexp_w + j0, X);
+      if (!b_exps_ready) rc = ozaki_operand_exponents(Bc, g.b.cs, g.b.rs, w, k, maxbits + m + j0, cexp_w + j0, X);
       if (rc) break;
       KernelTimer kt(MOMMS_KERNEL_PREP, X);
       ozaki_planes(ns, Bc, g.b.cs, g.b.rs, w, k, const_cast<__half*>(pb) + j0 * kp, kp, (int64_t)b_plane,
                    cexp_w + j0, X);
       note_launch();
+    }
+    if (verify) {
+      // B's magnitudes for the bound (verify implies B is not packed)
+      rc = enqueue_magnitudes(Bc, g.b.cs, g.b.rs, w, k, cexp_w + j0, bw.mag_b + j0 * bw.kp, bw.kp, bw.sum_b + j0, X);
+      if (rc) break;
+      if ((ce = cudaEventRecord(ev.mag[c], X)) != cudaSuccess || (ce = cudaStreamWaitEvent(V, ev.mag[c], 0)) != cudaSuccess) {
+        rc = cuda_fail(ce, "Ozaki bound events");
+        break;
+      }
     }
     CUtensorMap tmB, tmB_half;
     {
@@ -993,40 +1329,149 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       call_info().slice_variant = variant;
     }
     note_launch();
-    // C's columns j0..j1: recombination; with C staged from host memory and
-    // one chunk, in column ranges each copied back while the next is computed
-    ce = defer_c ? cudaStreamWaitEvent(X, ev_c[c], 0) : wait_operand(g, 2, X);
-    if (ce != cudaSuccess) {
-      rc = cuda_fail(ce, "operand staging");
-      break;
+    if (verify) {
+      // the recombination waits for the bound's verdict (below)
+      if ((ce = cudaEventRecord(ev.prod[c], X)) != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+    } else {
+      rc = combine_chunk(c, X);
     }
-    const int64_t nsub = (nch == 1 && stg && stg->writeback) ? std::min<int64_t>(4, w) : 1;
-    for (int64_t q = 0; q < nsub && !rc; ++q) {
-      cp.j0 = j0 + w * q / nsub;
-      cp.j1 = j0 + w * (q + 1) / nsub;
-      const int64_t bx = ceil_div(m, 512);
-      const int64_t by =
-          std::min<int64_t>({cp.j1 - cp.j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
-      {
-        KernelTimer kt(MOMMS_KERNEL_COMBINE, X);
-        combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, X>>>(cp);
+  }
+
+  // Verification: the bound kernel over all of C on V, once A's and every B
+  // chunk's magnitudes are in; the host reads the two maxima. Nothing has
+  // written C yet, so a count that misses the target is simply redone.
+  int redo = 0;
+  float q1f = 0.0f, q2f = 0.0f;
+  bool uncovered = false;
+  if (verify && !rc) {
+    rc = enqueue_bound_kernel(bw, m, n, k, false, ds->status, ds->sm_count, V);
+    if (!rc)
+      rc = bound_result(bw, OperandViews{A, g.a.rs, g.a.cs, B, g.b.rs, g.b.cs, rexp, cexp_w}, m, n, k, ds, V, &q1f,
+                        &q2f, &uncovered);
+    if (!rc) {
+      bool reachable = false;
+      const int need = guaranteed_slices(target, q1f, q2f, uncovered, &reachable);
+      if (need > ns) {
+        redo = need;  // more slices: redo with that count (C untouched)
+      } else {
+        call_info().bound_rel_err = uncovered ? HUGE_VAL : guaranteed_bound(ns, q1f, q2f);
+        if (!reachable) verdict = MOMMS_ERR_TARGET_UNREACHABLE;
       }
-      note_launch();
-      ce = launch_status();
-      if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki launch");
-      if (!rc) rc = columns_done(g, cp.j0, cp.j1, X);
+    }
+    for (int c = 0; c < nch && !rc && !redo; ++c) {
+      if ((ce = cudaStreamWaitEvent(V, ev.prod[c], 0)) != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
+      else rc = combine_chunk(c, V);
     }
   }
-  if (ev_fork) {
-    // s waits for the second stream's chunks (also after an error: the
-    // scratch freed below may still be in use there)
-    ce = cudaEventRecord(ev_join, ds->aux);
-    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(s, ev_join, 0);
-    if (!rc && ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki chunk streams");
-    cudaEventDestroy(ev_fork);
-    cudaEventDestroy(ev_join);
+  // s waits for the other streams' work (also after an error: the scratch
+  // the guards free may still be in use there)
+  if (nch > 1 || verify) {
+    cudaError_t e2 = cudaSuccess;
+    if (nch > 1) {
+      e2 = cudaEventRecord(ev.join, ds->aux);
+      if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, ev.join, 0);
+    }
+    if (e2 == cudaSuccess && verify) {
+      e2 = cudaEventRecord(ev.join2, V);
+      if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, ev.join2, 0);
+    }
+    if (!rc && e2 != cudaSuccess) rc = cuda_fail(e2, "Ozaki chunk streams");
   }
-  return rc;  // the guards return the scratch to the pool, in order on s after the join
+  ev.destroy();
+  if (rc) return rc;
+  if (redo) {
+    // Everything of this attempt is in flight or done on s; the operands are
+    // all on the device by now (every deferred copy was issued and s waits
+    // for it), so the repeat reads them in place, and C still holds its
+    // input values. The count comes from the bound: no sample, no second
+    // verification.
+    if (stg) {
+      // this attempt issued every deferred copy: s waits for C's (B's were
+      // waited for by the chunk streams s has joined), and the repeat finds
+      // both operands in place
+      for (int c = 0; c < nch && defer_c; ++c)
+        if (ev_c[c] && (ce = cudaStreamWaitEvent(s, ev_c[c], 0)) != cudaSuccess) return cuda_fail(ce, "operand staging");
+      stg->deferred[1] = stg->deferred[2] = false;
+      stg->ready[1] = stg->ready[2] = nullptr;
+    }
+    const int use = std::min(redo, kOzakiMaxSlices);
+    rc = launch_dgemm_ozaki(g, target, use, slices_used, s);
+    if (rc) return rc;
+    const double b = uncovered ? HUGE_VAL : guaranteed_bound(use, q1f, q2f);
+    call_info().bound_rel_err = b;
+    return b > target_or_fp64(target) ? MOMMS_ERR_TARGET_UNREACHABLE : MOMMS_OK;
+  }
+  return verdict;  // the guards return the scratch to the pool, in order on s after the joins
+}
+
+// The slice count of a plan's emulated problem, chosen once at plan creation
+// from the operands' current contents: the smallest count whose guaranteed
+// bound meets the target for every entry (exponents, magnitude planes and
+// the bound kernel, then one synchronisation). k beyond one launch's limit
+// is bounded slab by slab, as the launches compute it.
+int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
+  // a packed operand fixes the count
+  const PackedOperand* pa = packed_of(d.a);
+  const PackedOperand* pb = packed_of(d.b);
+  if (pa || pb) {
+    *slices = (pa ? pa : pb)->np;
+    return MOMMS_OK;
+  }
+  DeviceState* ds = device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  const int64_t m = d.m, n = d.n;
+  const int64_t nslab = ceil_div(d.k, kMaxK), kb = round_up(ceil_div(d.k, nslab), 64);
+  const int64_t kmax = std::min(d.k, kb);
+  void* ebuf = nullptr;
+  cudaError_t ce = scratch_alloc(&ebuf, (size_t)(m + n) * (sizeof(unsigned long long) + sizeof(int)), s);
+  if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
+  ScratchGuard free_ebuf(ebuf, s);
+  void* bw_mem = nullptr;
+  if ((ce = scratch_alloc(&bw_mem, bound_work_bytes(m, n, kmax), s)) != cudaSuccess)
+    return cuda_fail(ce, "Ozaki bound scratch");
+  ScratchGuard free_bw(bw_mem, s);
+  BoundWork bw{};
+  unsigned long long* maxbits = static_cast<unsigned long long*>(ebuf);
+  int* exps = reinterpret_cast<int*>(maxbits + (m + n));
+  int need = 1, rc = MOMMS_OK;
+  bool reachable_all = true;
+  for (int64_t p0 = 0; p0 < d.k && !rc; p0 += kb) {
+    DevGemm g;
+    g.m = m;
+    g.n = n;
+    g.k = std::min(kb, d.k - p0);
+    g.a = DevMat{static_cast<double*>(d.a.ptr) + p0 * d.a.cs, d.a.rs, d.a.cs};
+    g.b = DevMat{static_cast<double*>(d.b.ptr) + p0 * d.b.rs, d.b.rs, d.b.cs};
+    bound_work_carve(bw_mem, m, n, g.k, &bw);
+    rc = compute_exponents(g, maxbits, exps, s);
+    if (!rc) {
+      ce = cudaMemsetAsync(bw.sum_a, 0, (size_t)(m + n) * sizeof(unsigned long long) + 4 * sizeof(unsigned), s);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "Ozaki bound scratch");
+    }
+    const double* Ap = static_cast<const double*>(g.a.ptr);
+    const double* Bp = static_cast<const double*>(g.b.ptr);
+    if (!rc) rc = enqueue_magnitudes(Ap, g.a.rs, g.a.cs, m, g.k, exps, bw.mag_a, bw.kp, bw.sum_a, s);
+    if (!rc) rc = enqueue_magnitudes(Bp, g.b.cs, g.b.rs, n, g.k, exps + m, bw.mag_b, bw.kp, bw.sum_b, s);
+    if (!rc) rc = enqueue_bound_kernel(bw, m, n, g.k, false, ds->status, ds->sm_count, s);
+    float q1 = 0.0f, q2 = 0.0f;
+    bool uncovered = false;
+    if (!rc)
+      rc = bound_result(bw, OperandViews{Ap, g.a.rs, g.a.cs, Bp, g.b.rs, g.b.cs, exps, exps + m}, m, n, g.k, ds, s,
+                        &q1, &q2, &uncovered);
+    if (!rc) {
+      bool reachable = false;
+      need = std::max(need, guaranteed_slices(d.target_rel_err, q1, q2, uncovered, &reachable));
+      reachable_all = reachable_all && reachable;
+    }
+  }
+  if (rc) return rc;
+  *slices = need;
+  if (!reachable_all)
+    return fail(MOMMS_ERR_TARGET_UNREACHABLE,
+                "Ozaki: the requested error %.3g cannot be guaranteed for every entry with 15 slices (pass a fixed "
+                "slice count to run anyway)",
+                target_or_fp64(d.target_rel_err));
+  return MOMMS_OK;
 }
 
 }  // namespace momms

@@ -90,7 +90,7 @@ int momms_pack(int dtype, int precision, int role, int64_t rows, int64_t cols, c
     return fail(MOMMS_ERR_INVALID_ARG, "pack of %lld x %lld", (long long)rows, (long long)cols);
   if (src->mem == MOMMS_MEM_PACKED) return fail(MOMMS_ERR_INVALID_ARG, "source is already packed");
   if (!src->ptr || src->rs < 0 || src->cs < 0) return fail(MOMMS_ERR_INVALID_ARG, "bad source view");
-  if (precision == MOMMS_PREC_OZAKI && (slices < 0 || slices > 16))
+  if (precision == MOMMS_PREC_OZAKI && (slices < 0 || slices > kOzakiMaxSlices))
     return fail(MOMMS_ERR_INVALID_ARG, "slice count %d outside 0..16", slices);
   // k is the operand's inner dimension: A's columns, B's rows
   const int64_t K = role == MOMMS_ROLE_A ? cols : rows;

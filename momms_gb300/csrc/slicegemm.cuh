@@ -13,7 +13,7 @@
 // memory descriptors expect. Warp roles: warp 0 issues TMA, warp 1 (one
 // thread) issues tcgen05.mma and commits, warps 2..9 drain TMEM.
 //
-// Two epilogues:
+// Three epilogues:
 //   EPI_F32   : one group; finished chunks are summed in FP32 registers
 //               (round to nearest) and C = alpha*sum + beta*C is written at
 //               the end of the tile. Used by the split-TF32 f32 path (pairs
@@ -25,6 +25,18 @@
 //               exact sums are written to that group's int32 plane (the FP64
 //               recombination runs afterwards in its own kernel, so no FP64
 //               work sits in this pipeline).
+//   EPI_BOUND : one group of one pair, bf16 magnitude planes |a| 2^-e_i and
+//               |b| 2^-f_j rounded toward zero: the FP32 sum is a lower bound
+//               L_ij of (|A||B|)_ij 2^-(e_i+f_j) (after a factor for the
+//               accumulation's rounding). Nothing is stored per entry: each
+//               tile reduces the worst-case error ratios
+//                 q1 = (sum_p |a_ip| 2^-e_i + sum_p |b_pj| 2^-f_j) / L_ij,
+//                 q2 = k / L_ij
+//               (upward-rounded) to two maxima posted with atomicMax, and
+//               counts the entries with L_ij > 0, from which the host picks a
+//               slice count that holds for every entry. With count_only the
+//               planes are 0/1 indicators of nonzero elements and only the
+//               entries with a nonzero sum are counted.
 #pragma once
 #include <stdlib.h>
 
@@ -55,7 +67,7 @@ constexpr int TMEM_COLS = 512;  // two 128 x 256 f32 accumulators
 constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + 256;
 constexpr int MAX_GROUPS = 160, MAX_PAIRS = 160;
 
-enum { EPI_F32 = 0, EPI_OZAKI = 1 };
+enum { EPI_F32 = 0, EPI_OZAKI = 1, EPI_BOUND = 2 };
 
 struct Params {
   int64_t m, n;
@@ -85,6 +97,15 @@ struct Params {
   int* sbuf;
   int64_t plane;
   int64_t rsc, csc;
+  // EPI_BOUND: row sums of the scaled magnitudes of A (m) and B's columns
+  // (n) in units of 2^-40, each term rounded up; the lower-bound factor for
+  // the accumulation; k; the two maxima (bit patterns of non-negative floats)
+  const unsigned long long* msum_a;
+  const unsigned long long* msum_b;
+  float lb_scale, kf;
+  unsigned* bound_out;                // [0], [1]: the maxima
+  unsigned long long* bound_count;  // entries counted
+  int count_only;
   unsigned* status;
 };
 
@@ -128,6 +149,49 @@ __device__ __forceinline__ void drain_chunk(uint32_t taddr, EpiAcc<EPI> (&S)[NC]
       if (EPI == EPI_OZAKI) S[pc * 16 + j] += __float2int_rz(__uint_as_float(cur[j]));
       else S[pc * 16 + j] += __uint_as_float(cur[j]);
     }
+  }
+}
+
+// EPI_BOUND: this thread's row against its NC columns, reduced over the warp
+// and posted to the two maxima. Every lane calls it (rows past m contribute 0).
+template <int NC>
+__device__ __forceinline__ void bound_tile(const Params& p, int64_t row, int64_t col0, const float (&S)[NC]) {
+  float m1 = 0.0f, m2 = 0.0f;
+  unsigned cnt = 0;
+  if (row < p.m && p.count_only) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j) cnt += (col0 + j < p.n && S[j] > 0.0f) ? 1u : 0u;
+  } else if (row < p.m) {
+    const float sa = __fmul_ru(__ull2float_ru(p.msum_a[row]), 0x1p-40f);
+    float r2 = 0.0f;  // largest 1 / L over the row (q2 = k / L)
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+      const int64_t col = col0 + j;
+      const float lb = __fmul_rd(S[j], p.lb_scale);
+      // L = 0: no p with both a_ip and b_pj nonzero, so the entry has no error
+      if (col < p.n && lb > 0.0f) {
+        const float r = __frcp_ru(lb);  // >= 1 / L
+        const float sb = __fmul_ru(__ull2float_ru(p.msum_b[col]), 0x1p-40f);
+        m1 = fmaxf(m1, __fmul_ru(__fadd_ru(sa, sb), r));
+        r2 = fmaxf(r2, r);
+        ++cnt;
+      }
+    }
+    m2 = __fmul_ru(p.kf, r2);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative floats order like their bit patterns
+    if (!p.count_only) {
+      atomicMax(&p.bound_out[0], __float_as_uint(m1));
+      atomicMax(&p.bound_out[1], __float_as_uint(m2));
+    }
+    if (cnt) atomicAdd(p.bound_count, (unsigned long long)cnt);
   }
 }
 
@@ -248,7 +312,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else if (warp == 1) {
     // ------------------------------ MMA issuer ------------------------------
     if (lane == 0) {
-      const uint32_t idv = tc::idesc(KIND == 0 ? tc::FMT_F16 : tc::FMT_TF32, BM, BN);
+      const uint32_t idv = tc::idesc(tc::kind_fmt(KIND), BM, BN);
       int stage = 0;
       uint32_t ph = 0;
       int buf = 0;
@@ -380,6 +444,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
         }
       }
+      if constexpr (EPI == EPI_BOUND) bound_tile<EPI_COLS>(p, row, col0, S);
       if (EPI == EPI_F32 && row < p.m) {
         // C is read 8 columns at a time, every load of a group issued before
         // the first use (one memory round trip per group, not per element)
@@ -547,7 +612,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else if (warp == 1) {
     // ------------------------------ MMA issuer (even CTA) ------------------------------
     if (lane == 0 && leader) {
-      const uint32_t idv = tc::idesc(KIND == 0 ? tc::FMT_F16 : tc::FMT_TF32, 2 * BM, BN);
+      const uint32_t idv = tc::idesc(tc::kind_fmt(KIND), 2 * BM, BN);
       int stage = 0;
       uint32_t ph = 0;
       int buf = 0;
@@ -674,6 +739,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
         }
       }
+      if constexpr (EPI == EPI_BOUND) bound_tile<EPI_COLS>(p, row, col0, S);
       if (EPI == EPI_F32 && row < p.m) {
         // C is read 8 columns at a time, every load of a group issued before
         // the first use (one memory round trip per group, not per element)

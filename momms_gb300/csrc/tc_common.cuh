@@ -28,6 +28,11 @@ __device__ __forceinline__ uint64_t sdesc_k128(uint32_t smem_addr) {
 // (F16 = 0, BF16 = 1, TF32 = 2); bit 15/16 A/B major (0 = K-major);
 // [17,23) N >> 3; [24,29) M >> 4.
 constexpr uint32_t FMT_F16 = 0, FMT_BF16 = 1, FMT_TF32 = 2;
+// Operand kinds of the slice engine: 0 = fp16 and 2 = bf16 (both
+// tcgen05.mma kind::f16), 1 = tf32 (kind::tf32).
+__host__ __device__ constexpr uint32_t kind_fmt(int KIND) {
+  return KIND == 0 ? FMT_F16 : (KIND == 2 ? FMT_BF16 : FMT_TF32);
+}
 __host__ __device__ constexpr uint32_t idesc(uint32_t ab_fmt, int M, int N) {
   return (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
@@ -49,10 +54,10 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
 // ---- MMA: D[tmem] (+)= A[smem] * B[smem]^T, both K-major ----
-template <int KIND>  // 0 = kind::f16, 1 = kind::tf32
+template <int KIND>  // 0, 2 = kind::f16 (fp16, bf16 operands), 1 = kind::tf32
 __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc_v,
                                     uint32_t accumulate) {
-  if (KIND == 0) {
+  if (KIND != 1) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
@@ -96,7 +101,7 @@ __device__ __forceinline__ void tmem_dealloc2(uint32_t taddr, uint32_t ncols) {
 template <int KIND>
 __device__ __forceinline__ void mma2(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc_v,
                                      uint32_t accumulate) {
-  if (KIND == 0) {
+  if (KIND != 1) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"

@@ -43,7 +43,7 @@ def test_abi_version(lib):
 
 
 def test_status_strings(lib):
-    for code in range(0, 10):
+    for code in range(0, 11):
         s = lib.momms_status_string(code).decode()
         assert s and s != "unknown status"
     assert lib.momms_status_string(12345).decode() == "unknown status"
