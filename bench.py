@@ -22,10 +22,11 @@ The metric is FP64 GEMM throughput at FP64 accuracy, plain vs emulated:
           run), on a bounded sample of the same workload.
   batched : 512 uneven problems as one captured grouped plan vs one launch
           per problem;
-  serving : the served request stream (Poisson arrivals, mixed sizes and
-          modes) with p50/p99 latency and throughput against the offline
-          grouped run of the same requests (served_p50_ms / served_p99_ms
-          repeat the first rate's figures).
+  serving : the served request stream (2000 requests per rate, Poisson
+          arrivals, mixed sizes and modes) with p50/p99 latency and throughput
+          against the offline grouped run of the same requests;
+          served_p50_ms / served_p99_ms are those of the lowest rate whose
+          served throughput reaches 0.8 of the offline run.
 
 --impl reference runs only that CPU algorithm, with every host thread, and
 prints its own line.
@@ -385,11 +386,13 @@ def measure_batched(lib, mg, torch, dev):
             "launches_per_batch": "one graph launch (one persistent kernel per dtype)"}
 
 
-def measure_serving(lib, mg, torch, dev, rates=(400.0, 1600.0), count=300):
+def measure_serving(lib, mg, torch, dev, rates=(400.0, 1600.0, 3200.0), count=2000):
     """Poisson arrivals of mixed requests (m, n, k log-uniform over [64, 4096];
     40% f64 plain, 40% f64 emulated at a 1e-14 target, 20% f32) with operands
     resident in HBM under a 60 GiB budget; latency percentiles and throughput
-    against the offline grouped run of the same request set."""
+    against the offline grouped run of the same request set, at each rate, and
+    per run the largest number of launches whose device intervals overlapped
+    (CUDA events on the server's streams around each launch)."""
     descs, keep, flops = _problem_set(mg, torch, dev, count, 64, 4096, 5, [0.4, 0.4, 0.2])
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
@@ -404,19 +407,33 @@ def measure_serving(lib, mg, torch, dev, rates=(400.0, 1600.0), count=300):
         srv = ctypes.c_void_p()
         mg.check(lib.momms_server_create(ctypes.byref(cfg), ctypes.byref(srv)), lib)
         arrivals = np.cumsum(np.random.default_rng(9).exponential(1.0 / rate, count))
+        ids = []
         t0 = time.perf_counter()
         for i in range(count):
             while time.perf_counter() - t0 < arrivals[i]:
                 pass
             rid = ctypes.c_uint64(0)
             mg.check(lib.momms_server_submit(srv, ctypes.byref(descs[i]), ctypes.byref(rid)), lib)
+            ids.append(rid.value)
         mg.check(lib.momms_server_drain(srv, 300.0), lib)
         rep = mg.ServerReport()
         lib.momms_server_stats(srv, ctypes.byref(rep), 0)
+        intervals = {}
+        for rid in ids:
+            info = mg.RequestInfo()
+            lib.momms_server_poll(srv, rid, ctypes.byref(info))
+            intervals[info.batch_id] = (info.device_start_ms, info.device_end_ms)
         lib.momms_server_destroy(srv)
+        # most launches in flight on the device at once (sweep over interval ends)
+        edges = sorted([(s, 1) for s, e in intervals.values()] + [(e, -1) for s, e in intervals.values()])
+        depth = most = 0
+        for _, step in edges:
+            depth += step
+            most = max(most, depth)
         runs.append({"rate_per_s": rate, "p50_ms": rep.p50_ms, "p99_ms": rep.p99_ms, "mean_ms": rep.mean_ms,
                      "tflops": rep.tflops, "vs_offline_grouped": rep.tflops / offline, "batches": rep.batches,
-                     "mean_batch": rep.mean_batch, "completed": rep.completed, "failed": rep.failed})
+                     "mean_batch": rep.mean_batch, "completed": rep.completed, "failed": rep.failed,
+                     "most_launches_overlapping_on_device": most})
     del keep
     return {"workload": f"{count} requests, Poisson arrivals, m,n,k log-uniform [64,4096] (seed 5), "
                         "40% f64 plain / 40% f64 emulated (1e-14) / 20% f32, 60 GiB admission budget",
@@ -673,9 +690,14 @@ def run_ours(args):
         line["serving"] = measure_serving(lib, mg, torch, dev)
         line["out_of_core"] = measure_out_of_core(lib, mg, torch)
         line["packed"] = measure_packed(lib, mg, torch)
+        # the served latency is quoted at the lowest swept rate whose served
+        # throughput reaches 0.8 of the offline grouped run (the last rate if none does)
         serving_runs = line["serving"]["runs"]
-        line["served_p50_ms"] = serving_runs[0]["p50_ms"]
-        line["served_p99_ms"] = serving_runs[0]["p99_ms"]
+        quoted = next((r for r in serving_runs if r["vs_offline_grouped"] >= 0.8), serving_runs[-1])
+        line["served_p50_ms"] = quoted["p50_ms"]
+        line["served_p99_ms"] = quoted["p99_ms"]
+        line["served_rate_per_s"] = quoted["rate_per_s"]
+        line["served_vs_offline_grouped"] = quoted["vs_offline_grouped"]
     bits = ctypes.c_uint32(0)
     lib.momms_device_status(ctypes.byref(bits))
     line["device_status_bits"] = bits.value

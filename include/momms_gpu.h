@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define MOMMS_ABI_VERSION 1
+#define MOMMS_ABI_VERSION 2
 
 typedef enum {
   MOMMS_OK = 0,
@@ -247,6 +247,9 @@ typedef struct {
   double submit_s, start_s, done_s; /* seconds on the server's clock */
   int32_t status;                   /* momms_status of the request */
   int32_t batch_size;               /* requests in the launch it ran in */
+  uint64_t batch_id;                /* the launch it ran in (numbered from 1) */
+  double device_start_ms;           /* that launch's device interval: CUDA events on its stream before and */
+  double device_end_ms;             /* after it, in ms after the server started (-1 if it failed) */
 } momms_request_info;
 typedef struct {
   uint64_t submitted, completed, rejected, failed, batches;

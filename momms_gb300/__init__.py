@@ -82,7 +82,8 @@ class ServerConfig(ctypes.Structure):
 
 class RequestInfo(ctypes.Structure):
     _fields_ = [("submit_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
-                ("status", ctypes.c_int32), ("batch_size", ctypes.c_int32)]
+                ("status", ctypes.c_int32), ("batch_size", ctypes.c_int32), ("batch_id", ctypes.c_uint64),
+                ("device_start_ms", ctypes.c_double), ("device_end_ms", ctypes.c_double)]
 
 
 class ServerReport(ctypes.Structure):

@@ -12,7 +12,10 @@
 // overlaps on the device. Every problem is planned from its own shape and
 // data only, so a result is bit-identical alone and in any mix. Latency is
 // measured on the host from submission to the moment the scheduler sees the
-// batch's completion event.
+// batch's completion event. Each batch also carries two timing events on its
+// stream, around its launch: their times relative to an event recorded when
+// the server starts are the batch's device interval, reported per request, so
+// that the overlap of batches on the GPU can be read off directly.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -37,14 +40,18 @@ struct Request {
   int status = MOMMS_OK;
   int batch_size = 0;
   bool done = false;
+  uint64_t batch_id = 0;
+  double dev_start_ms = -1.0, dev_end_ms = -1.0;  // the batch's device interval
 };
 
 struct Batch {
   std::vector<uint64_t> ids;
   Plan* plan = nullptr;
-  cudaEvent_t ev = nullptr;
+  cudaEvent_t ev_start = nullptr;  // before the launch, on the batch's stream
+  cudaEvent_t ev = nullptr;        // after it: the batch is done when this completes
   int stream = 0;
   bool big = false;
+  uint64_t id = 0;
 };
 
 // Requests estimated to run longer than this alone are "large".
@@ -86,6 +93,8 @@ struct Server {
   int launching = 0;  // batches taken from `ready` and not yet in `inflight`
   int big_inflight = 0;
   int sm_count = 0;
+  cudaEvent_t ev0 = nullptr;  // the device clock's origin for batch intervals
+  uint64_t next_batch = 1;
 
   bool idle() const { return pending.empty() && ready.empty() && inflight.empty() && launching == 0; }
   std::thread th;
@@ -132,8 +141,21 @@ struct Server {
           continue;
         }
         const int st = (q == cudaSuccess) ? MOMMS_OK : cuda_fail(q, "batch");
-        for (uint64_t id : b.ids) finish_request(id, st, (int)b.ids.size());
+        float t_start = -1.0f, t_end = -1.0f;
+        if (st == MOMMS_OK && (cudaEventElapsedTime(&t_start, ev0, b.ev_start) != cudaSuccess ||
+                               cudaEventElapsedTime(&t_end, ev0, b.ev) != cudaSuccess)) {
+          cudaGetLastError();
+          t_start = t_end = -1.0f;
+        }
+        for (uint64_t id : b.ids) {
+          Request& r = reqs[id];
+          r.batch_id = b.id;
+          r.dev_start_ms = t_start;
+          r.dev_end_ms = t_end;
+          finish_request(id, st, (int)b.ids.size());
+        }
         plan_destroy(b.plan);
+        cudaEventDestroy(b.ev_start);
         cudaEventDestroy(b.ev);
         stream_busy[b.stream] = 0;
         if (b.big) big_inflight -= 1;
@@ -197,13 +219,15 @@ struct Server {
         lk.unlock();
         cudaStream_t s = streams[sidx];
         int rc = plan_create(descs.data(), (int)descs.size(), &b.plan, s, true);
-        if (!rc) rc = plan_launch(b.plan, s, max_sms);
         cudaError_t e = cudaSuccess;
         if (!rc) {
-          e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming);
-          if (e == cudaSuccess) e = cudaEventRecord(b.ev, s);
+          e = cudaEventCreate(&b.ev_start);
+          if (e == cudaSuccess) e = cudaEventCreate(&b.ev);
+          if (e == cudaSuccess) e = cudaEventRecord(b.ev_start, s);
           if (e != cudaSuccess) rc = cuda_fail(e, "batch event");
         }
+        if (!rc) rc = plan_launch(b.plan, s, max_sms);
+        if (!rc && (e = cudaEventRecord(b.ev, s)) != cudaSuccess) rc = cuda_fail(e, "batch event");
         // A batch that failed after some of its work was enqueued is finished
         // only when that work is: its requests' outputs are not touched again
         // once they are reported.
@@ -212,12 +236,14 @@ struct Server {
         launching -= 1;
         if (rc) {
           if (b.plan) plan_destroy(b.plan);
+          if (b.ev_start) cudaEventDestroy(b.ev_start);
           if (b.ev) cudaEventDestroy(b.ev);
           for (uint64_t id : b.ids) finish_request(id, rc, (int)b.ids.size());
           stream_busy[sidx] = 0;
           if (b.big) big_inflight -= 1;
           cv_done.notify_all();
         } else {
+          b.id = next_batch++;
           batches += 1;
           batched += b.ids.size();
           inflight.push_back(std::move(b));
@@ -266,6 +292,15 @@ int momms_server_create(const momms_server_config* cfg, momms_server* out) {
     }
     sv->streams.push_back(s);
     sv->stream_busy.push_back(0);
+  }
+  cudaError_t e0 = cudaEventCreate(&sv->ev0);
+  if (e0 == cudaSuccess) e0 = cudaEventRecord(sv->ev0, sv->streams[0]);
+  if (e0 == cudaSuccess) e0 = cudaEventSynchronize(sv->ev0);
+  if (e0 != cudaSuccess) {
+    for (cudaStream_t t : sv->streams) cudaStreamDestroy(t);
+    if (sv->ev0) cudaEventDestroy(sv->ev0);
+    delete sv;
+    return cuda_fail(e0, "server clock event");
   }
   sv->th = std::thread([sv] { sv->loop(); });
   *out = new momms_server_s{sv};
@@ -329,6 +364,9 @@ static void fill_info(const momms::Request& r, momms_request_info* info) {
   info->done_s = r.done_s;
   info->status = r.status;
   info->batch_size = r.batch_size;
+  info->batch_id = r.batch_id;
+  info->device_start_ms = r.dev_start_ms;
+  info->device_end_ms = r.dev_end_ms;
 }
 
 int momms_server_poll(momms_server server, uint64_t id, momms_request_info* info) {
@@ -433,6 +471,7 @@ int momms_server_destroy(momms_server server) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
   }
+  if (sv->ev0) cudaEventDestroy(sv->ev0);
   delete sv;
   delete server;
   return MOMMS_OK;

@@ -39,7 +39,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.momms_abi_version() == 1
+    assert lib.momms_abi_version() == 2
 
 
 def test_status_strings(lib):

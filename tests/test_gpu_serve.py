@@ -68,16 +68,20 @@ def test_served_results_equal_alone_and_batches_overlap(gpu):
     for rid in ids:
         info = mg.RequestInfo()
         mg.check(gpu.momms_server_wait(srv, rid, 60.0, ctypes.byref(info)), gpu)
-        infos.append((info.submit_s, info.start_s, info.done_s, info.batch_size))
+        infos.append((info.submit_s, info.start_s, info.done_s, info.batch_size, info.batch_id,
+                      info.device_start_ms, info.device_end_ms))
     rep = mg.ServerReport()
     mg.check(gpu.momms_server_stats(srv, ctypes.byref(rep), 0), gpu)
     assert rep.completed == len(reqs) and rep.failed == 0 and rep.rejected == 0
     assert rep.batches >= 2 and rep.p50_ms > 0 and rep.p99_ms >= rep.p50_ms
-    # continuous batching: some request started before an earlier batch ended
-    starts = sorted(x[1] for x in infos)
-    dones = sorted(x[2] for x in infos)
-    assert starts[-1] < dones[-1]
-    assert any(s < dones[0] for s in starts[1:]) or rep.batches >= 3
+    # continuous batching: two launches' device intervals (CUDA events on
+    # their streams around each launch) intersect, so their work overlapped
+    # on the GPU
+    batches = sorted({(x[4], x[5], x[6]) for x in infos})
+    assert len(batches) == rep.batches and all(0 <= s < e for _, s, e in batches)
+    overlapping = [(a, b) for i, a in enumerate(batches) for b in batches[i + 1:]
+                   if max(a[1], b[1]) < min(a[2], b[2])]
+    assert overlapping, batches
     mg.check(gpu.momms_server_destroy(srv), gpu)
     torch.cuda.synchronize()
     for (d, t, h) in reqs:
