@@ -299,8 +299,7 @@ typedef struct {
   int32_t groups;         /* OZAKI: accumulation groups */
   int32_t splits;         /* plain paths: k splits */
   int32_t slice_variant;  /* tensor-core paths: slice kernel variant run: 0 = one CTA per tile,
-                             2 = CTA pairs with one cta_group::2 MMA, 3 = OZAKI fused pair kernel (the
-                             recombination in the epilogue, small k; 1 is unused) */
+                             2 = CTA pairs with one cta_group::2 MMA (1 is unused) */
   double bound_rel_err;   /* OZAKI with an automatic slice count: a rigorous bound on
                              max_ij |dC_ij| / (|A||B|)_ij of the product, over every entry (-1 otherwise) */
 } momms_call_info;

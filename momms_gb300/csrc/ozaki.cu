@@ -373,6 +373,46 @@ struct CombineParams {
   int64_t rsc, csc;
 };
 
+// Nearest double to a 128-bit signed integer times 2^scale.
+__device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
+  if (R == 0) return 0.0;
+  const bool neg = R < 0;
+  unsigned __int128 U = neg ? (unsigned __int128)(-R) : (unsigned __int128)R;
+  const unsigned long long hi = (unsigned long long)(U >> 64);
+  unsigned long long top;
+  int sh = 0;
+  if (hi == 0) {
+    top = (unsigned long long)U;
+  } else {
+    sh = 64 - __clzll((long long)hi);  // significant bits above the low word
+    top = (unsigned long long)(U >> sh);
+    const unsigned __int128 rest = U & (((unsigned __int128)1 << sh) - 1);
+    if (rest != 0) top |= 1ull;  // sticky bit: top keeps 64 significant bits
+  }
+  // Round top to 53 significant bits (nearest, ties to even) and place the
+  // exponent directly: integer instructions only, since GB300's FP64 pipe is
+  // narrow. Same result as converting top to double (the only rounding) and
+  // scaling by 2^(sh + scale) exactly, which is what the rare results outside
+  // the normal range still do.
+  const int lz = __clzll((long long)top);
+  const unsigned long long t = top << lz;  // bit 63 set
+  unsigned long long mant = t >> 11;
+  const unsigned rb = (unsigned)(t & 0x7ffull);
+  if (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ++mant;
+  int E = 63 - lz + sh + scale;  // value = (mant / 2^52) * 2^E
+  if (mant >> 53) {
+    mant >>= 1;
+    ++E;
+  }
+  if (E < -1022 || E > 1023) {
+    const double v = __ull2double_rn(top);
+    return ldexp(neg ? -v : v, sh + scale);
+  }
+  const unsigned long long b = ((unsigned long long)(E + 1023) << 52) | (mant & ((1ull << 52) - 1)) |
+                               (neg ? (1ull << 63) : 0ull);
+  return __longlong_as_double((long long)b);
+}
+
 // Thread rows i and i + 256 of block row blockIdx.x, for columns
 // j0 + blockIdx.y, stepping by gridDim.y: no index division, the row
 // exponents stay in registers, and the two rows' loads are in flight together.
@@ -451,7 +491,7 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
       if (u == 1 && !two) break;
       double v;
       if (er[u] == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-      else v = sp::i128_to_double((__int128)(u == 0 ? R0 : R1), er[u] + ec + p.scale_off);
+      else v = i128_to_double((__int128)(u == 0 ? R0 : R1), er[u] + ec + p.scale_off);
       double* cp = p.c + rows[u] * p.rsc + j * p.csc;
       const double sv = p.alpha_one ? v : v * p.alpha;  // v * 1 == v: one FP64 operation saved
       *cp = p.beta_zero ? sv : fma(p.beta, c_old[u], sv);
@@ -537,7 +577,6 @@ void ozaki_operand_planes(int ns, const double* x, int64_t sr, int64_t sp, int64
 int set_attrs_ozaki() {
   cudaError_t e = sp::set_slice_attrs<0, sp::EPI_OZAKI>();
   if (e == cudaSuccess) e = sp::set_slice_attrs<2, sp::EPI_BOUND>();
-  if (e == cudaSuccess) e = sp::set_fused_attrs();
   return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "cudaFuncSetAttribute(Ozaki)");
 }
 
@@ -916,23 +955,6 @@ struct Events {
   }
 };
 
-// Whether an emulated call runs the fused kernel: k up to kFusedMaxK (beyond
-// it the products are tensor-bound and the 256-wide tiles of the unfused
-// kernel feed the tensor cores better than the fused kernel's 64-wide ones;
-// the separate recombination is then a few per cent of the call), at most 12
-// slices (the recombination's exact 128-bit sum then needs no tail terms), and
-// at least two m-tiles (CTA pairs). MOMMS_OZAKI_FUSED=0 / 1 forces the choice
-// for A/B runs (1 still needs the structural conditions); results are the
-// same bits either way.
-constexpr int64_t kFusedMaxK = 2048;
-bool use_fused(int64_t m, int64_t k, int ns, bool verify) {
-  if (verify || ns > kHornerLevels + 1 || m <= sp::BM) return false;
-  const char* env = getenv("MOMMS_OZAKI_FUSED");
-  if (env && env[0] == '0') return false;
-  if (env && env[0] == '1') return true;
-  return k <= kFusedMaxK;
-}
-
 }  // namespace
 
 int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_used, cudaStream_t s) {
@@ -1154,16 +1176,12 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   call_info().pairs = np;
   call_info().groups = ng;
 
-  // Small k: the fused kernel recombines each tile in its epilogue (no group
-  // planes). Not under verification, whose recombination waits for the
-  // bound's verdict.
-  const bool fused = use_fused(m, k, ns, verify);
   int* sbuf = nullptr;
   // group planes tile-blocked (sp::Params::sbuf): m and n padded to whole
   // 128 x 256 tiles, each tile one contiguous block
   const int64_t mpad = round_up(m, (int64_t)sp::BM);
   const size_t plane = (size_t)mpad * (size_t)round_up(n, (int64_t)sp::BN);
-  if (!fused && (ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
+  if ((ce = scratch_alloc(&sbuf, (size_t)ng * plane * sizeof(int), s)) != cudaSuccess)
     return cuda_fail(ce, "Ozaki group sums");
   ScratchGuard free_sbuf(sbuf, s);
   p.plane = (int64_t)plane;
@@ -1204,18 +1222,7 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     cp.scale_off = -2 * bits - bits * dmax;
     cp.alpha_one = (g.alpha == 1.0);
     cp.beta_zero = (g.beta == 0.0);
-    // the fused epilogue's form of the same sum: group g enters R shifted by
-    // 8 (dmax - level); no tail groups (use_fused keeps ns - 1 <= dmax)
-    for (int gi = 0; gi < ng; ++gi) p.group_shift[gi] = (uint8_t)(bits * (dmax - dgrp[gi]));
-    p.scale_off = cp.scale_off;
-    p.alpha_one = cp.alpha_one;
-    p.beta_zero = cp.beta_zero;
   }
-  p.alpha = g.alpha;
-  p.beta = g.beta;
-  p.rsc = g.c.rs;
-  p.csc = g.c.cs;
-  p.row_exp = rexp;
   cp.m = m;
   cp.row_exp = rexp;
   cp.col_exp = cexp;
@@ -1308,38 +1315,6 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
       if (rc) break;
     }
     p.n = w;
-    if (fused) {
-      // products and recombination of columns j0..j1 in one kernel, which
-      // reads and writes C: C's columns must be in
-      ce = defer_c ? cudaStreamWaitEvent(X, ev_c[c], 0) : wait_operand(g, 2, X);
-      if (ce != cudaSuccess) {
-        rc = cuda_fail(ce, "operand staging");
-        break;
-      }
-      CUtensorMap tmBq;
-      uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)w, (uint64_t)ns};
-      uint64_t stridesb[2] = {(uint64_t)kp * 2, (uint64_t)b_plane * 2};
-      uint32_t boxq[3] = {64, (uint32_t)sp::F_B_ROWS, 1};
-      rc = encode_tiled(&tmBq, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, pb + j0 * kp, dimsb, stridesb, boxq,
-                        CU_TENSOR_MAP_SWIZZLE_128B);
-      if (rc) break;
-      p.tiles_n = (int)ceil_div(w, sp::F_BN);
-      p.c64 = static_cast<double*>(g.c.ptr) + j0 * g.c.cs;
-      p.col_exp = cexp + j0;
-      {
-        KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, X);
-        ce = sp::launch_fused<0>(tmA, tmBq, p, X);
-        if (ce == cudaSuccess) ce = launch_status();
-      }
-      note_launch();
-      if (ce != cudaSuccess) {
-        rc = cuda_fail(ce, "Ozaki fused launch");
-        break;
-      }
-      call_info().slice_variant = 3;
-      rc = columns_done(g, j0, j1, X);
-      continue;
-    }
     p.tiles_n = (int)ceil_div(w, sp::BN);
     p.sbuf = sbuf + j0 * mpad;  // j0 is a multiple of the tile width: the chunk's tile blocks start here
     {

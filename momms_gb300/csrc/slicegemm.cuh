@@ -106,63 +106,10 @@ struct Params {
   unsigned* bound_out;                // [0], [1]: the maxima
   unsigned long long* bound_count;  // entries counted
   int count_only;
-  // Fused Ozaki kernel: the recombination in the epilogue. Group g's exact
-  // sums enter R with weight 2^group_shift[g] (8 * (dmax - level)); then
-  // C = beta*C + alpha * 2^(e_i + f_j + scale_off) * R, as the recombination
-  // kernel computes it.
-  uint8_t group_shift[MAX_GROUPS];
-  int scale_off;
-  int alpha_one, beta_zero;
-  double alpha, beta;
-  double* c64;
-  const int* row_exp;
-  const int* col_exp;
   unsigned* status;
 };
 
 __device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0; }
-
-// Nearest double to a 128-bit signed integer times 2^scale: the one rounding
-// of an emulated product (used by the recombination kernel and by the fused
-// epilogue, so that both give the same bits).
-__device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
-  if (R == 0) return 0.0;
-  const bool neg = R < 0;
-  unsigned __int128 U = neg ? (unsigned __int128)(-R) : (unsigned __int128)R;
-  const unsigned long long hi = (unsigned long long)(U >> 64);
-  unsigned long long top;
-  int sh = 0;
-  if (hi == 0) {
-    top = (unsigned long long)U;
-  } else {
-    sh = 64 - __clzll((long long)hi);  // significant bits above the low word
-    top = (unsigned long long)(U >> sh);
-    const unsigned __int128 rest = U & (((unsigned __int128)1 << sh) - 1);
-    if (rest != 0) top |= 1ull;  // sticky bit: top keeps 64 significant bits
-  }
-  // Round top to 53 significant bits (nearest, ties to even) and place the
-  // exponent directly: integer instructions only, since GB300's FP64 pipe is
-  // narrow. Same result as converting top to double (the only rounding) and
-  // scaling by 2^(sh + scale) exactly, which is what the rare results outside
-  // the normal range still do.
-  const int lz = __clzll((long long)top);
-  const unsigned long long t = top << lz;  // bit 63 set
-  unsigned long long mant = t >> 11;
-  const unsigned rb = (unsigned)(t & 0x7ffull);
-  if (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ++mant;
-  int E = 63 - lz + sh + scale;  // value = (mant / 2^52) * 2^E
-  if (mant >> 53) {
-    mant >>= 1;
-    ++E;
-  }
-  if (E < -1022 || E > 1023) {
-    const double v = __ull2double_rn(top);
-    return ldexp(neg ? -v : v, sh + scale);
-  }
-  const unsigned long long b = ((unsigned long long)(E + 1023) << 52) | (mant & ((1ull << 52) - 1)) |
-                               (neg ? (1ull << 63) : 0ull);
-  return __longlong_as_double((long long)b);
-}
 
 // Output tile of work item t: groups of 16 m-tiles swept n-tile by n-tile,
 // so that the ~152 tiles in flight at once share 16 A row panels and about
@@ -830,315 +777,6 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Fused Ozaki kernel (CTA pairs, cta_group::2, 256 x 64 pair tiles): all slice
-// products of a tile, group by group, and then the recombination into C in
-// the epilogue, with no group sums in HBM. Each epilogue thread owns one row
-// and F_COLS columns of its CTA's 128 x 64 half and keeps, per entry, the
-// exact sum R = sum_g S_g 2^group_shift[g] in a 128-bit integer: every TMEM
-// chunk it drains (an exact integer, |c| <= 2^24) is added with its group's
-// shift. At the end of the tile R is rounded once to FP64 and scaled, and
-// C = beta*C + alpha*value is written: the integer and the rounding of the
-// recombination kernel, so the results are bit-identical to the unfused path.
-// 64 output columns per pair keep R in registers (128 of them); the price is
-// shared-memory bandwidth per MMA (A is read once per 64 output columns
-// instead of 256), which calls with small k, bound by C's traffic and the
-// epilogue rather than the tensor cores, do not pay for. Four TMEM
-// accumulators of 64 columns let the MMAs run ahead of the drains.
-//   full[s]   (even CTA)  both CTAs' TMA loads complete here (40 KB)
-//   empty[s]  (each CTA)  the even CTA's commit, multicast: stage s is free
-//   tfull[b]  (each CTA)  the even CTA's commit, multicast: accumulator b done
-//   tempty[b] (even CTA)  all 16 epilogue warps of the pair: b drained
-// ---------------------------------------------------------------------------
-constexpr int F_BN = 64;
-constexpr int F_B_ROWS = F_BN / 2;                            // B rows each CTA of a pair stages
-constexpr int F_STAGE_BYTES = A_TILE + F_B_ROWS * ROW_BYTES;  // 20 KB (1024-byte multiple)
-constexpr int F_STAGES = 10;
-constexpr int F_BUFS = 4;
-constexpr int F_TMEM_COLS = F_BUFS * F_BN;        // 256
-constexpr int F_COLS = F_BN / (EPI_WARPS / 4);    // 32 columns per epilogue thread
-constexpr int F_SMEM_BYTES = 1024 + F_STAGES * F_STAGE_BYTES + 512;
-static_assert(F_STAGE_BYTES % 1024 == 0, "stages must keep the 1024-byte swizzle alignment");
-
-// Adds 16 drained chunk values with weight 2^(32 W + b) to R[j0 .. j0+15].
-template <int W>
-__device__ __forceinline__ void fold16(unsigned __int128 (&R)[F_COLS], int j0, const uint32_t (&v)[16], int b) {
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const long long t = (long long)__float2int_rz(__uint_as_float(v[j])) << b;  // |t| < 2^55
-    R[j0 + j] += (unsigned __int128)((__int128)t << (32 * W));
-  }
-}
-
-template <int KIND>
-__global__ void __launch_bounds__(THREADS, 1)
-    slice_fused_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBq,
-                            const __grid_constant__ Params p) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + F_STAGES * F_STAGE_BYTES);
-  uint64_t* empty = full + F_STAGES;
-  uint64_t* tfull = empty + F_STAGES;  // [F_BUFS]
-  uint64_t* tempty = tfull + F_BUFS;   // [F_BUFS]
-  uint64_t* drain = tempty + F_BUFS;   // used only when aborting
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t rank = cluster_ctarank();
-  const bool leader = (rank == 0);
-  const int64_t unit0 = (int64_t)cluster_id_x(), unit_step = (int64_t)cluster_count_x();
-  const int units_m = (p.tiles_m + 1) / 2;
-  const int64_t units = (int64_t)units_m * p.tiles_n;  // tiles_n counts 64-wide tiles
-  auto unit_at = [&](int64_t r) { return r * unit_step + ((r & 1) ? (unit_step - 1 - unit0) : unit0); };
-  auto coords = [&](int64_t t, int& tm, int& tn) {
-    int um;
-    tile_coords<8>(t, units_m, p.tiles_n, um, tn);
-    tm = 2 * um + (int)rank;  // rank 1 of an odd last pair reads zero rows, writes nothing
-  };
-
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < F_STAGES; ++i) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], 1);
-    }
-    for (int b = 0; b < F_BUFS; ++b) {
-      mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 2 * EPI_WARPS);
-    }
-    mbar_init(drain, 1);
-    *abort_flag = 0;
-    fence_barrier_init();
-  }
-  if (warp == 1) {
-    tc::tmem_alloc2(tmem_slot, F_TMEM_COLS);
-    tc::tmem_relinquish2();
-  }
-  tc::fence_before();
-  __syncthreads();
-  cluster_sync();  // the pair's barriers exist before any remote arrival
-  tc::fence_after();
-  const uint32_t tmem_base = *tmem_slot;
-
-  if (warp == 0) {
-    // ------------------------------ TMA producer (both CTAs) ------------------------------
-    if (lane == 0) {
-      prefetch_tensormap(&tmA);
-      prefetch_tensormap(&tmBq);
-      int stage = 0;
-      uint32_t ph = 0;
-      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-        const int64_t t = unit_at(r);
-        if (t >= units) continue;
-        int tm, tn;
-        coords(t, tm, tn);
-        for (int pi = 0; pi < p.group_begin[p.ngroups]; ++pi) {
-          for (int kb = 0; kb < p.kblocks; ++kb) {
-            if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
-              report_status(p.status, DEV_TIMEOUT_EMPTY);
-              *abort_flag = 1;
-              goto producer_done;
-            }
-            if (leader) mbar_arrive_expect_tx(&full[stage], 2 * F_STAGE_BYTES);
-            uint8_t* sa = smem + stage * F_STAGE_BYTES;
-            const uint32_t bar = mapa_shared(&full[stage], 0);
-            tma_load_3d_pair(sa, &tmA, bar, kb * p.kelems, tm * BM, p.pair_a[pi]);
-            tma_load_3d_pair(sa + A_TILE, &tmBq, bar, kb * p.kelems, tn * F_BN + (int)rank * F_B_ROWS,
-                             p.pair_b[pi]);
-            if (++stage == F_STAGES) {
-              stage = 0;
-              ph ^= 1;
-            }
-          }
-        }
-      }
-      if (!aborted(abort_flag)) {
-        // every stage released: no commit from the even CTA is still on its
-        // way to this CTA's barriers
-        for (int i = 0; i < F_STAGES; ++i) {
-          if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
-            report_status(p.status, DEV_TIMEOUT_EMPTY);
-            *abort_flag = 1;
-            break;
-          }
-          if (++stage == F_STAGES) {
-            stage = 0;
-            ph ^= 1;
-          }
-        }
-      }
-    producer_done:;
-    }
-  } else if (warp == 1) {
-    // ------------------------------ MMA issuer (even CTA) ------------------------------
-    if (lane == 0 && leader) {
-      const uint32_t idv = tc::idesc(tc::kind_fmt(KIND), 2 * BM, F_BN);
-      int stage = 0;
-      uint32_t ph = 0;
-      int buf = 0;
-      uint32_t acc_ph[F_BUFS] = {};
-      auto close = [&]() {
-        tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
-        acc_ph[buf] ^= 1;
-        buf = (buf + 1) % F_BUFS;
-      };
-      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-        const int64_t t = unit_at(r);
-        if (t >= units) continue;
-        for (int g = 0; g < p.ngroups; ++g) {
-          int load = 0;
-          bool open = false;
-          uint32_t d_tmem = 0;
-          for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-            const int w = p.pair_w[pp];
-            if (open && !p.merge_pairs) {
-              close();
-              open = false;
-            }
-            for (int st = 0; st < p.kblocks;) {
-              if (open && load + w > p.chunk_cap) {
-                close();
-                open = false;
-              }
-              bool fresh = false;
-              if (!open) {
-                if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-                  report_status(p.status, DEV_TIMEOUT_TMEM);
-                  *abort_flag = 1;
-                  goto mma_done;
-                }
-                tc::fence_after();
-                d_tmem = tmem_base + (uint32_t)(buf * F_BN);
-                load = 0;
-                open = fresh = true;
-              }
-              const int s0 = st, s1 = min(p.kblocks, st + (p.chunk_cap - load) / w);
-              for (; st < s1; ++st) {
-                if (!mbar_wait_bounded(&full[stage], ph)) {
-                  report_status(p.status, DEV_TIMEOUT_FULL);
-                  *abort_flag = 1;
-                  goto mma_done;
-                }
-                tc::fence_after();
-                const uint32_t a_addr = smem_u32(smem + stage * F_STAGE_BYTES);
-                const uint32_t b_addr = a_addr + A_TILE;
-#pragma unroll
-                for (int kk = 0; kk < KSTEPS; ++kk)
-                  tc::mma2<KIND>(d_tmem, tc::sdesc_k128(a_addr + kk * 32), tc::sdesc_k128(b_addr + kk * 32), idv,
-                                (fresh && st == s0 && kk == 0) ? 0u : 1u);
-                tc::commit2_mc(&empty[stage], (uint16_t)0x3);
-                if (++stage == F_STAGES) {
-                  stage = 0;
-                  ph ^= 1;
-                }
-              }
-              load += (s1 - s0) * w;
-            }
-          }
-          if (open) close();
-        }
-      }
-    mma_done:
-      if (aborted(abort_flag)) {
-        tc::commit2_mc(drain, (uint16_t)0x1);
-        mbar_wait_bounded(drain, 0);
-      }
-    }
-  } else {
-    // ------------------------------ epilogue (both CTAs) ------------------------------
-    const int q = warp & 3;
-    const int h = (warp - 2) >> 2;
-    const int r_local = q * 32 + lane;
-    uint32_t tempty_leader[F_BUFS];
-#pragma unroll
-    for (int b = 0; b < F_BUFS; ++b) tempty_leader[b] = mapa_shared(&tempty[b], 0);
-    int buf = 0;
-    uint32_t acc_ph[F_BUFS] = {};
-    for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-      const int64_t t = unit_at(r);
-      if (t >= units) continue;
-      int tm, tn;
-      coords(t, tm, tn);
-      const int64_t row = (int64_t)tm * BM + r_local;
-      const int64_t col0 = (int64_t)tn * F_BN + h * F_COLS;
-      // C's lines for this tile, asked of L2 now and read at the end: a
-      // warp's 32 rows of one column of column-major C are two 128-byte lines
-      if (!p.beta_zero && p.rsc == 1 && (int64_t)tm * BM + q * 32 < p.m && col0 + lane < p.n) {
-        const double* cl = p.c64 + ((int64_t)tm * BM + q * 32) + (col0 + lane) * p.csc;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(cl));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(cl + 16));
-      }
-      unsigned __int128 R[F_COLS];
-#pragma unroll
-      for (int j = 0; j < F_COLS; ++j) R[j] = 0;
-      for (int g = 0; g < p.ngroups; ++g) {
-        const int sh = p.group_shift[g];
-        const int wsh = sh >> 5, bsh = sh & 31;
-        for (int c = 0; c < p.group_chunks[g]; ++c) {
-          if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-            report_status(p.status, DEV_TIMEOUT_MMA);
-            *abort_flag = 1;
-            goto epi_done;
-          }
-          tc::fence_after();
-          const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * F_BN + h * F_COLS);
-#pragma unroll
-          for (int half = 0; half < F_COLS / 16; ++half) {
-            uint32_t v[16];
-            tc::ld16(taddr + half * 16, v);
-            tc::ld_wait(v);
-            if (wsh == 0) fold16<0>(R, half * 16, v, bsh);
-            else if (wsh == 1) fold16<1>(R, half * 16, v, bsh);
-            else fold16<2>(R, half * 16, v, bsh);
-          }
-          tc::fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive_cluster_relaxed(tempty_leader[buf]);
-          acc_ph[buf] ^= 1;
-          buf = (buf + 1) % F_BUFS;
-        }
-      }
-      if (row < p.m) {
-        // the recombination: one rounding of the exact sum, the scale, alpha
-        // and beta (C's loads of 8 columns in flight together)
-        const int er = p.row_exp[row];
-        double* crow = p.c64 + row * p.rsc;
-#pragma unroll
-        for (int j0 = 0; j0 < F_COLS; j0 += 8) {
-          double c_old[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int64_t col = col0 + j0 + j;
-            c_old[j] = (!p.beta_zero && col < p.n) ? crow[col * p.csc] : 0.0;
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int64_t col = col0 + j0 + j;
-            if (col < p.n) {
-              const int ec = p.col_exp[col];
-              double v;
-              if (er == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-              else v = i128_to_double((__int128)R[j0 + j], er + ec + p.scale_off);
-              const double sv = p.alpha_one ? v : v * p.alpha;
-              crow[col * p.csc] = p.beta_zero ? sv : fma(p.beta, c_old[j], sv);
-            }
-          }
-        }
-      }
-    }
-  epi_done:;
-  }
-
-  __syncwarp();
-  tc::fence_before();
-  __syncthreads();
-  cluster_sync();  // both CTAs are done with each other's barriers and TMEM
-  if (warp == 1) {
-    tc::fence_after();
-    tc::tmem_dealloc2(tmem_base, F_TMEM_COLS);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 // Chunk counts of every group (Params::group_chunks) under the chunk rule
@@ -1183,11 +821,6 @@ inline cudaError_t set_slice_attrs() {
     e = cudaFuncSetAttribute(slice_gemm_pair_kernel<KIND, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              P_SMEM_BYTES);
   return e;
-}
-
-inline cudaError_t set_fused_attrs() {
-  return cudaFuncSetAttribute(slice_fused_pair_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              F_SMEM_BYTES);
 }
 
 // Kernel variants: 0 = one CTA per tile, 2 = CTA pairs with cta_group::2 MMA
@@ -1297,34 +930,6 @@ inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_f
   const int grid = (int)std::min<int64_t>(units, sm_count);
   slice_gemm_kernel<KIND, EPI><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, q);
   return cudaGetLastError();
-}
-
-// Fused Ozaki launch (pair tiles of 256 x 64; needs two m-tiles and the
-// pair kernel on this device): tmBq is B's map with boxes of F_B_ROWS rows.
-// Returns cudaErrorNotSupported where CTA pairs cannot be scheduled.
-template <int KIND>
-inline cudaError_t launch_fused(const CUtensorMap& tmA, const CUtensorMap& tmBq, const Params& p, cudaStream_t s) {
-  cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = cluster2_config(F_SMEM_BYTES, attr);
-  static std::atomic<int> cache_n[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  int clusters = cache_n[dev].load();
-  if (clusters == 0) {
-    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)slice_fused_pair_kernel<KIND>, &cfg) != cudaSuccess) {
-      cudaGetLastError();
-      clusters = -1;
-    }
-    if (clusters <= 0) clusters = -1;
-    cache_n[dev].store(clusters);
-  }
-  if (clusters < 0 || p.tiles_m < 2) return cudaErrorNotSupported;
-  Params q = p;
-  if (!plan_chunks(q)) return cudaErrorInvalidValue;
-  const int64_t units = (int64_t)((p.tiles_m + 1) / 2) * p.tiles_n;
-  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
-  cfg.stream = s;
-  return cudaLaunchKernelEx(&cfg, slice_fused_pair_kernel<KIND>, tmA, tmBq, q);
 }
 
 }  // namespace sp
