@@ -368,9 +368,10 @@ typedef enum {
 int momms_timing_enable(int on);
 int momms_timing_read(int kernel_class, double* total_ms, unsigned long long* launches, int reset);
 
-/* Measures the current device's peak issue rate in TFLOP/s with a
- * register-only loop: kind 0 = FP64 tensor-core MMA (DMMA m8n8k4),
- * kind 1 = FP32 FFMA. The roofline denominators of the f64 and f32 plain
+/* Measures the current device's peak issue rate in TFLOP/s (TOP/s for
+ * kind 2) with a register-only loop: kind 0 = FP64 tensor-core MMA (DMMA
+ * m8n8k4), kind 1 = FP32 FFMA, kind 2 = the legacy INT8 tensor path
+ * (mma.sync m16n8k32 s8 -> s32, the alternative to fp16 digits on tcgen05). The roofline denominators of the f64 and f32 plain
  * paths. No reference counterpart (the reference only reports GFLOP/s,
  * src/util.rs:94-97). Synchronises the device. */
 int momms_measure_peak(int kind, double* tflops);

@@ -46,9 +46,6 @@ constexpr int kDigitBits = 8;
 // single pair's int32 sum stays below 2^31 for up to 511 k-blocks of 64
 constexpr int64_t kMaxK = kOzakiMaxK;
 static_assert((kMaxK / 64) * 64 * (1ll << (2 * kDigitBits)) < (1ll << 31), "int32 digit sums must stay exact");
-// Horner levels combined exactly: with at most 16 groups of |S| < 2^31 per
-// level, R stays below 2^(36 + bits*dmax) < 2^127
-constexpr int kHornerLevels = (127 - 36) / kDigitBits;
 // an int32 group sum's bound (sums of the pairs' worst cases)
 constexpr double kGroupLimit = 2147483647.0;
 // one TMEM chunk's bound: integers up to 2^24 are exact in FP32
@@ -344,24 +341,26 @@ __global__ void __launch_bounds__(32) sample_final_kernel(const double* __restri
 // Recombination of the exact group sums. Group g holds S_g = the int32 sum of
 // the digit products of diagonal d_g (weight 2^(-bits*(d_g-2))), so
 //   R = sum_g S_g * 2^(bits*(dmax - (d_g-2)))
-// is an exact integer (below 2^(30 + bits*dmax + log2 groups) < 2^127), and
+// is an exact integer (below 2^(31 + bits*dmax + 3): 2^147 at 15 slices), and
 //   C = beta*C + alpha * 2^(e_i + f_j - 2 bits - bits*dmax) * R
 // with R rounded to double once. All the summation is integer arithmetic;
 // FP64 is used for the final conversion, scaling and beta update only.
+//
+// R is formed from four 64-bit partial sums, one per 32-bit word offset:
+// group g's weight 2^sh (sh = bits*(dmax - level) <= 112) is split into a
+// word gw[g] = sh / 32 and a shift gb[g] = sh % 32 <= 24, so that
+// R = P0 + P1 2^32 + P2 2^64 + P3 2^96 with P_w = sum over the groups of word
+// w of S_g 2^gb[g]: each term is below 2^55 and a word holds at most four
+// levels (at most eight groups each), so no partial sum leaves 64 bits. Every
+// level enters exactly, up to the most slices (dmax = 14), and R is rounded
+// once (wide_to_double).
 struct CombineParams {
   const int* sbuf;  // tile-blocked group planes (sp::Params::sbuf)
   int64_t plane;
   int64_t mpad;     // m rounded up to the slice kernel's tile height
-  // Horner over the levels L = d_g - 2 <= dmax: entry q multiplies R by
-  // 2^(bits * hsh[q]) and then adds group hg[q]'s S_g (hg[q] == 255: none).
-  // Groups below dmax (lower diagonals; dmax = min(largest level, 12) keeps R below
-  // 2^127) are added as S_g >> tail_sh.
-  int nh;
-  uint8_t hg[2 * sp::MAX_GROUPS];
-  uint8_t hsh[2 * sp::MAX_GROUPS];  // 0 or 1
-  int ntail;
-  uint8_t tail_g[sp::MAX_GROUPS];
-  uint8_t tail_sh[sp::MAX_GROUPS];
+  int ng;
+  uint8_t gw[sp::MAX_GROUPS];  // word offset of group g (0..3)
+  uint8_t gb[sp::MAX_GROUPS];  // left shift within the word
   int scale_off;  // -2 bits - bits*dmax
   int alpha_one, beta_zero;
   int64_t m;
@@ -413,6 +412,29 @@ __device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
   return __longlong_as_double((long long)b);
 }
 
+// Nearest double to R * 2^scale, R = P0 + P1 2^32 + P2 2^64 + P3 2^96 exactly
+// (|R| < 2^148). R below 2^126 in magnitude goes through i128_to_double as
+// is; a wider R is first shifted right to 126 bits with the lost bits kept
+// as a sticky bit 0 (more than the 53 + 2 bits the rounding looks at), which
+// leaves the rounded result unchanged.
+__device__ __forceinline__ double wide_to_double(long long P0, long long P1, long long P2, long long P3, int scale) {
+  const __int128 low = (__int128)P0 + ((__int128)P1 << 32);        // |.| < 2^93
+  const __int128 hi = (__int128)P2 + ((__int128)P3 << 32) + (low >> 64);  // R = hi 2^64 + lo, lo in [0, 2^64)
+  const unsigned long long lo = (unsigned long long)low;
+  const __int128 lim = (__int128)1 << 61;
+  if (hi >= -lim && hi < lim) return i128_to_double((__int128)(((unsigned __int128)hi << 64) | lo), scale);
+  const bool neg = hi < 0;
+  // the magnitude as uh 2^64 + ul
+  unsigned __int128 uh = neg ? (unsigned __int128)(-hi) - (lo != 0 ? 1u : 0u) : (unsigned __int128)hi;
+  const unsigned long long ul = neg ? (0ull - lo) : lo;
+  const unsigned long long uh_hi = (unsigned long long)(uh >> 64), uh_lo = (unsigned long long)uh;
+  const int nbh = uh_hi ? 128 - __clzll((long long)uh_hi) : 64 - __clzll((long long)uh_lo);  // bits of uh (>= 62)
+  const int s = nbh + 64 - 126;  // 1..22: the magnitude has nbh + 64 bits
+  unsigned __int128 u = (uh << (64 - s)) | (unsigned __int128)(ul >> s);
+  if (ul & ((1ull << s) - 1)) u |= 1u;  // sticky
+  return i128_to_double(neg ? -(__int128)u : (__int128)u, scale + s);
+}
+
 // Thread rows i and i + 256 of block row blockIdx.x, for columns
 // j0 + blockIdx.y, stepping by gridDim.y: no index division, the row
 // exponents stay in registers, and the two rows' loads are in flight together.
@@ -441,57 +463,49 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
       c_old[0] = p.c[rows[0] * p.rsc + j * p.csc];
       if (two) c_old[1] = p.c[rows[1] * p.rsc + j * p.csc];
     }
-    // two's complement in unsigned 128-bit arithmetic
-    u128 R0 = 0, R1 = 0;
-    if (p.nh <= kCombineBatch) {
-      // all loads first (up to 2 x kCombineBatch in flight), then the Horner steps
+    // the four 64-bit partial sums of each of the two rows (see CombineParams)
+    long long P0[2] = {0, 0}, P1[2] = {0, 0}, P2[2] = {0, 0}, P3[2] = {0, 0};
+    auto add = [&](int u, int s_g, int g) {
+      const int w = p.gw[g];
+      const long long t = (long long)s_g << p.gb[g];
+      if (w == 0) P0[u] += t;
+      else if (w == 1) P1[u] += t;
+      else if (w == 2) P2[u] += t;
+      else P3[u] += t;
+    };
+    if (p.ng <= kCombineBatch) {
+      // all loads first (up to 2 x kCombineBatch in flight), then the sums
       int s0[kCombineBatch], s1[kCombineBatch];
 #pragma unroll
       for (int q = 0; q < kCombineBatch; ++q) {
         s0[q] = 0;
         s1[q] = 0;
-        if (q < p.nh && p.hg[q] != 255) {
-          const int* sg = col + (int64_t)p.hg[q] * p.plane;
+        if (q < p.ng) {
+          const int* sg = col + (int64_t)q * p.plane;
           s0[q] = sg[roff[0]];
           if (two) s1[q] = sg[roff[1]];
         }
       }
 #pragma unroll
       for (int q = 0; q < kCombineBatch; ++q) {
-        if (q < p.nh) {
-          if (p.hsh[q]) {  // next level: one constant shift
-            R0 <<= bits;
-            R1 <<= bits;
-          }
-          R0 += (u128)(__int128)s0[q];
-          R1 += (u128)(__int128)s1[q];
+        if (q < p.ng) {
+          add(0, s0[q], q);
+          add(1, s1[q], q);
         }
       }
     } else {
-      for (int q = 0; q < p.nh; ++q) {
-        if (p.hsh[q]) {
-          R0 <<= bits;
-          R1 <<= bits;
-        }
-        const int g = p.hg[q];
-        if (g != 255) {
-          const int* sg = col + (int64_t)g * p.plane;
-          R0 += (u128)(__int128)sg[roff[0]];
-          if (two) R1 += (u128)(__int128)sg[roff[1]];
-        }
+      for (int q = 0; q < p.ng; ++q) {
+        const int* sg = col + (int64_t)q * p.plane;
+        add(0, sg[roff[0]], q);
+        if (two) add(1, sg[roff[1]], q);
       }
-    }
-    for (int q = 0; q < p.ntail; ++q) {
-      const int* sg = col + (int64_t)p.tail_g[q] * p.plane;
-      R0 += (u128)(__int128)(sg[roff[0]] >> p.tail_sh[q]);
-      if (two) R1 += (u128)(__int128)(sg[roff[1]] >> p.tail_sh[q]);
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       if (u == 1 && !two) break;
       double v;
       if (er[u] == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-      else v = i128_to_double((__int128)(u == 0 ? R0 : R1), er[u] + ec + p.scale_off);
+      else v = wide_to_double(P0[u], P1[u], P2[u], P3[u], er[u] + ec + p.scale_off);
       double* cp = p.c + rows[u] * p.rsc + j * p.csc;
       const double sv = p.alpha_one ? v : v * p.alpha;  // v * 1 == v: one FP64 operation saved
       *cp = p.beta_zero ? sv : fma(p.beta, c_old[u], sv);
@@ -1191,34 +1205,14 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   cp.plane = (int64_t)plane;
   cp.mpad = mpad;
   {
-    // Horner entries in level order: a shift by one level between levels
-    // (an empty level only shifts), then each group of the level
-    const int dmax = std::min(ns - 1, kHornerLevels);
-    int nh = 0;
-    for (int L = 0; L <= dmax; ++L) {
-      bool first = true;
-      for (int gi = 0; gi < ng; ++gi)
-        if (dgrp[gi] == L) {
-          cp.hg[nh] = (uint8_t)gi;
-          cp.hsh[nh] = (uint8_t)((first && L > 0) ? 1 : 0);
-          ++nh;
-          first = false;
-        }
-      if (first && L > 0) {  // no group at this level
-        cp.hg[nh] = 255;
-        cp.hsh[nh] = 1;
-        ++nh;
-      }
+    // each group's weight 2^(bits*(dmax - level)) as (word, shift)
+    const int dmax = ns - 1;
+    cp.ng = ng;
+    for (int gi = 0; gi < ng; ++gi) {
+      const int sh = bits * (dmax - dgrp[gi]);
+      cp.gw[gi] = (uint8_t)(sh >> 5);
+      cp.gb[gi] = (uint8_t)(sh & 31);
     }
-    cp.nh = nh;
-    cp.ntail = 0;
-    for (int gi = 0; gi < ng; ++gi)
-      if (dgrp[gi] > dmax) {
-        cp.tail_g[cp.ntail] = (uint8_t)gi;
-        // floor(S / 2^sh); for |S| < 2^31 a shift by 31 already gives it
-        cp.tail_sh[cp.ntail] = (uint8_t)std::min(31, bits * (dgrp[gi] - dmax));
-        ++cp.ntail;
-      }
     cp.scale_off = -2 * bits - bits * dmax;
     cp.alpha_one = (g.alpha == 1.0);
     cp.beta_zero = (g.beta == 0.0);

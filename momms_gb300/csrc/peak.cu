@@ -33,6 +33,28 @@ __global__ void dmma_peak_loop(double* out, int iters) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The legacy integer tensor path (mma.sync m16n8k32, s8 x s8 -> s32): the
+// alternative an INT8 Ozaki scheme would run on, since tcgen05 has no integer
+// kind on sm_103a. 2*16*8*32 operations per instruction.
+__global__ void imma_peak_loop(int* out, int iters) {
+  int c[kAcc][4];
+  const uint32_t a0 = 0x01020304u + threadIdx.x, b0 = 0x05060708u ^ threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < kAcc; ++j) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int j = 0; j < kAcc; ++j)
+      asm volatile(
+          "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+          : "+r"(c[j][0]), "+r"(c[j][1]), "+r"(c[j][2]), "+r"(c[j][3])
+          : "r"(a0), "r"(a0 + 1), "r"(a0 + 2), "r"(a0 + 3), "r"(b0), "r"(b0 + 1));
+  }
+  int s = 0;
+#pragma unroll
+  for (int j = 0; j < kAcc; ++j) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 __global__ void ffma_peak_loop(float* out, int iters) {
   float c[kAcc];
   const float a = 1.0f + threadIdx.x * 1e-7f, b = 0.9999f;
@@ -59,7 +81,7 @@ unsigned long long momms_launch_count(void) { return momms::g_launches.load(); }
 
 int momms_measure_peak(int kind, double* tflops) {
   using namespace momms;
-  if (!tflops || kind < 0 || kind > 1) return fail(MOMMS_ERR_INVALID_ARG, "momms_measure_peak: bad argument");
+  if (!tflops || kind < 0 || kind > 2) return fail(MOMMS_ERR_INVALID_ARG, "momms_measure_peak: bad argument");
   DeviceState* ds = device_state();
   if (!ds) return MOMMS_ERR_NO_DEVICE;
   const int blocks = ds->sm_count * 4, threads = 256;
@@ -69,12 +91,13 @@ int momms_measure_peak(int kind, double* tflops) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int iters = kind == 0 ? 1500 : 40000;
+  const int iters = kind == 0 ? 1500 : (kind == 1 ? 40000 : 20000);
   float best_ms = 1e30f;
   for (int rep = 0; rep < 3; ++rep) {
     cudaEventRecord(e0);
     if (kind == 0) dmma_peak_loop<<<blocks, threads>>>(static_cast<double*>(out), iters);
-    else ffma_peak_loop<<<blocks, threads>>>(static_cast<float*>(out), iters);
+    else if (kind == 1) ffma_peak_loop<<<blocks, threads>>>(static_cast<float*>(out), iters);
+    else imma_peak_loop<<<blocks, threads>>>(static_cast<int*>(out), iters);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -86,8 +109,10 @@ int momms_measure_peak(int kind, double* tflops) {
   cudaEventDestroy(e1);
   cudaFree(out);
   if (e != cudaSuccess) return cuda_fail(e, "peak probe");
-  const double flops = kind == 0 ? (double)blocks * (threads / 32) * iters * kAcc * 512.0
-                                 : (double)blocks * threads * iters * kAcc * 2.0;
+  const double warp_steps = (double)blocks * (threads / 32) * iters * kAcc;
+  const double flops = kind == 0   ? warp_steps * 512.0
+                       : kind == 1 ? (double)blocks * threads * iters * kAcc * 2.0
+                                   : warp_steps * 8192.0;
   *tflops = flops / (best_ms * 1e-3) / 1e12;
   return MOMMS_OK;
 }

@@ -8,7 +8,8 @@ Every entry of C is checked against the double-double oracle (no sampling):
 * square 2048^3 in all four modes;
 * the emulation inputs a = U[-0.5,0.5] exp(phi N(0,1)) at 2048^3 for
   phi = 0.5, 2, 8: fixed slice counts 3..9 (error falling as slices are
-  added) and the automatic count at a 1e-14 target, met on every entry;
+  added) and the automatic count at a 1e-14 target, met on every entry or
+  reported unreachable with a bound that holds;
 * one FFMA call whose operand offsets pass 2^32 elements (the kernel's 64-bit
   offset path).
 
@@ -117,9 +118,20 @@ def test_emulation_inputs_slice_sweep_and_automatic_count(gpu, phi):
         if 8 * U64 < a < 1e-3:
             assert b < a / 16, errs
     rc, C, info = _device_call(gpu, A, B, C0, mg.PREC_OZAKI, target_rel_err=1e-14)
-    assert rc == mg.OK, gpu.momms_last_error()
-    assert info.bound_rel_err <= 1e-14
-    assert ou.rel_err(C, ref, mag) <= 1e-14
+    err = ou.rel_err(C, ref, mag)
+    if rc == mg.ERR_TARGET_UNREACHABLE:
+        # wide spreads (phi = 8: about 2^80 between a row's largest and
+        # smallest entries) put entries out of reach of per-row / per-column
+        # power-of-two scaling: the call says so, with the 15-slice result and
+        # the bound that holds for it
+        assert info.slices == 15 and info.bound_rel_err > 1e-14
+        assert err <= info.bound_rel_err + 4 * U64
+        print(f"phi={phi}: target unreachable, bound {info.bound_rel_err:.3g}, measured {err:.3g}")
+    else:
+        assert rc == mg.OK, gpu.momms_last_error()
+        assert info.bound_rel_err <= 1e-14
+        assert err <= 1e-14
+        print(f"phi={phi}: {info.slices} slices, bound {info.bound_rel_err:.3g}, measured {err:.3g}")
 
 
 def test_ffma_offsets_beyond_32_bits(gpu):
