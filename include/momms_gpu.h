@@ -274,18 +274,28 @@ int momms_server_destroy(momms_server server);
 
 /* ---- Autotuning -----------------------------------------------------------
  * The runtime analogue of the reference's compile-time block sizes
- * (typenum NC/KC/MC/MR/NR, src/exper/l3_packing.rs:58-66): times the split-k
- * candidates of a plain problem on its device operands (writing only a scratch
- * C) and records the fastest in a process-wide table keyed by
- * (dtype, precision, m, n, k) that momms_gemm and plans consult. Synchronous. */
+ * (typenum NC/KC/MC/MR/NR, src/exper/l3_packing.rs:58-66): times the launch
+ * configurations of a plain problem on its device operands (writing only a
+ * scratch C) — every output tile the dtype's kernel has (f32: 128 x 128 with
+ * two CTAs per SM, or 64 x 64 with eight), each with the k-split counts that
+ * keep two k-blocks per split — and records the fastest in a process-wide
+ * table keyed by shape bucket (dtype, precision, ceil(log2) of m, n and k)
+ * that momms_gemm and plans consult. A configuration never changes which
+ * products are summed in which order inside a split, and a problem's entry
+ * does not depend on its batch. Synchronous. */
 typedef struct {
   int32_t splits;     /* chosen k-split count */
   int32_t candidates; /* configurations timed */
   float best_ms;      /* time of the chosen configuration */
-  int32_t reserved;
+  int32_t tile;       /* chosen output tile: 0 = 128 x 128, 1 = the small tile (f32: 64 x 64) */
 } momms_tune_result;
 int momms_autotune(const momms_gemm_desc* desc, momms_tune_result* out, void* stream);
-/* Table as text, one "dtype precision m n k splits" line per entry. */
+/* Tunes every shape bucket of a batch once (the bucket's first plain problem
+ * stands for it); *tuned (may be null) receives the number of buckets timed. */
+int momms_autotune_batch(const momms_gemm_desc* descs, int count, void* stream, int* tuned);
+/* Table as text, one "dtype precision m n k splits tile" line per entry
+ * (m, n, k: the bucket's largest shape; on import any shape of the bucket,
+ * and the tile field may be left out for 0). */
 int momms_tune_export(char* buf, size_t cap, size_t* needed);
 int momms_tune_import(const char* text);
 int momms_tune_clear(void);

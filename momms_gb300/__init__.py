@@ -72,7 +72,7 @@ class CallInfo(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("splits", ctypes.c_int32), ("candidates", ctypes.c_int32), ("best_ms", ctypes.c_float),
-                ("reserved", ctypes.c_int32)]
+                ("tile", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -173,6 +173,8 @@ def load_library(path=None):
     lib.momms_server_destroy.restype = i32
     lib.momms_autotune.argtypes = [PD, ctypes.POINTER(TuneResult), vp]
     lib.momms_autotune.restype = i32
+    lib.momms_autotune_batch.argtypes = [PD, i32, vp, ctypes.POINTER(ctypes.c_int32)]
+    lib.momms_autotune_batch.restype = i32
     lib.momms_tune_export.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
     lib.momms_tune_export.restype = i32
     lib.momms_tune_import.argtypes = [ctypes.c_char_p]

@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(dmma::THREADS, 1)
   }
 }
 
-template <typename Off>
-__global__ void __launch_bounds__(ffma::THREADS, 2)
+template <int TM, typename Off>
+__global__ void __launch_bounds__(ffma::Tile<TM>::THREADS, ffma::Tile<TM>::CTAS_PER_SM)
     sgemm_grouped_kernel(const SProblem* __restrict__ probs, int nprobs, int64_t total_units,
                          unsigned long long* next_unit, float* partials, unsigned* counters) {
   using namespace ffma;
@@ -192,11 +192,11 @@ __global__ void __launch_bounds__(ffma::THREADS, 2)
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-    prefetch_c_tile(P.e, tm, tn);
-    ffma_unit_any<Off>(P.o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
-    ffma_finish(P.e, acc, tm, tn, P.splits, sp,
-                P.splits > 1 ? partials + P.part_offset + (size_t)tile * P.splits * BM * BN : nullptr,
-                P.splits > 1 ? counters + P.counter_offset + tile : nullptr, &s_last);
+    prefetch_c_tile<TM>(P.e, tm, tn);
+    ffma_unit_any<TM, Off>(P.o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
+    ffma_finish<TM>(P.e, acc, tm, tn, P.splits, sp,
+                    P.splits > 1 ? partials + P.part_offset + (size_t)tile * P.splits * TM * TM : nullptr,
+                    P.splits > 1 ? counters + P.counter_offset + tile : nullptr, &s_last);
   }
   // the last CTA out resets the unit counter for the next launch of the plan
   __syncthreads();
@@ -237,14 +237,17 @@ struct Plan {
   double* d_partials = nullptr;
   unsigned* d_counters = nullptr;
   unsigned long long* d_next = nullptr;  // unit counter + finished-CTA counter
-  // f32 plain group
-  int ns = 0;
-  int64_t s_units = 0;
-  grouped::SProblem* s_probs = nullptr;
-  float* s_partials = nullptr;
-  unsigned* s_counters = nullptr;
-  unsigned long long* s_next = nullptr;
-  bool s_wide = false;  // some f32 operand needs 64-bit element offsets
+  // f32 plain groups, one per FFMA tile (0: 128 x 128, 1: 64 x 64), each
+  // one persistent launch
+  struct SGroup {
+    int ns = 0;
+    int64_t units = 0;
+    grouped::SProblem* probs = nullptr;
+    float* partials = nullptr;
+    unsigned* counters = nullptr;
+    unsigned long long* next = nullptr;
+    bool wide = false;  // some f32 operand needs 64-bit element offsets
+  } sg[2];
   // problems run by their own launch sequence (Ozaki, split-TF32)
   std::vector<PlanProblem> other;
   // operands copied to column-major scratch before each launch (f64
@@ -482,10 +485,10 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
     if (rc) { plan_free(p); return rc; }
   }
 
-  // ---- f32 group ----
+  // ---- f32 groups: each problem's tile (tuning table or model) decides its group ----
   if (!slist.empty()) {
     using namespace ffma;
-    std::vector<std::pair<double, grouped::SProblem>> items;
+    std::vector<std::pair<double, grouped::SProblem>> items[2];
     for (int i : slist) {
       const momms_gemm_desc& d = descs[i];
       const DevGemm gv = devgemm_of(d);  // packed operands: their column-major copies
@@ -504,48 +507,54 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
                        a_ld % 4 == 0 && b_ld % 4 == 0;
       P.o = Operands{static_cast<const float*>(va.ptr), va.rs, va.cs, static_cast<const float*>(vb.ptr), vb.rs,
                      vb.cs, d.m, d.n, d.k, a_xc, b_xc, vec};
-      if (!offsets_fit_32(P.o)) p->s_wide = true;
       P.e = Epi{d.m, d.n, (float)d.alpha, (float)d.beta, static_cast<float*>(d.c.ptr), d.c.rs, d.c.cs};
-      P.tiles_m = (int)ceil_div(d.m, BM);
-      P.tiles_n = (int)ceil_div(d.n, BN);
+      const PlainCfg cfg = plain_cfg(MOMMS_DTYPE_F32, d.m, d.n, d.k, ds->sm_count);
+      const int TMv = cfg.tile == 1 ? 64 : 128;
+      if (!offsets_fit_32(P.o)) p->sg[cfg.tile].wide = true;
+      P.tiles_m = (int)ceil_div(d.m, TMv);
+      P.tiles_n = (int)ceil_div(d.n, TMv);
       const int64_t kb = ceil_div(d.k, BK);
-      const double tile_cost = (double)std::min<int64_t>(d.m, BM) * std::min<int64_t>(d.n, BN) * (double)kb;
-      int s = splits_f32(d.m, d.n, d.k, ds->sm_count);
-      P.kb_split = ceil_div(kb, s);
+      const double tile_cost = (double)std::min<int64_t>(d.m, TMv) * std::min<int64_t>(d.n, TMv) * (double)kb;
+      P.kb_split = ceil_div(kb, cfg.splits);
       P.splits = (int)ceil_div(kb, P.kb_split);
-      items.push_back({tile_cost / P.splits, P});
+      items[cfg.tile].push_back({tile_cost / P.splits, P});
     }
-    std::sort(items.begin(), items.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-    std::vector<grouped::SProblem> probs;
-    int64_t units = 0, parts = 0, ctrs = 0;
-    for (auto& it : items) {
-      grouped::SProblem P = it.second;
-      const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
-      P.unit_begin = units;
-      units += tiles * P.splits;
-      if (P.splits > 1) {
-        P.part_offset = parts;
-        P.counter_offset = ctrs;
-        parts += tiles * P.splits * BM * BN;
-        ctrs += tiles;
+    for (int t = 0; t < 2; ++t) {
+      if (items[t].empty()) continue;
+      const int TMv = t == 1 ? 64 : 128;
+      Plan::SGroup& G = p->sg[t];
+      std::sort(items[t].begin(), items[t].end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+      std::vector<grouped::SProblem> probs;
+      int64_t units = 0, parts = 0, ctrs = 0;
+      for (auto& it : items[t]) {
+        grouped::SProblem P = it.second;
+        const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
+        P.unit_begin = units;
+        units += tiles * P.splits;
+        if (P.splits > 1) {
+          P.part_offset = parts;
+          P.counter_offset = ctrs;
+          parts += tiles * P.splits * TMv * TMv;
+          ctrs += tiles;
+        }
+        probs.push_back(P);
       }
-      probs.push_back(P);
+      G.ns = (int)probs.size();
+      G.units = units;
+      void* buf;
+      int rc = plan_alloc(p, &buf, probs.size() * sizeof(grouped::SProblem));
+      if (!rc) { G.probs = static_cast<grouped::SProblem*>(buf); rc = plan_alloc(p, &buf, (size_t)parts * 4); }
+      if (!rc) { G.partials = static_cast<float*>(buf); rc = plan_alloc(p, &buf, (size_t)ctrs * 4 + 16); }
+      if (!rc) { G.counters = static_cast<unsigned*>(buf); rc = plan_alloc(p, &buf, 2 * sizeof(unsigned long long)); }
+      if (!rc) G.next = static_cast<unsigned long long*>(buf);
+      if (rc) { plan_free(p); return rc; }
+      const size_t off = p->host_tables.size();
+      rc = plan_upload(p, G.probs, probs.data(), probs.size() * sizeof(grouped::SProblem));
+      if (!rc && async) pending.push_back({G.probs, {off, probs.size() * sizeof(grouped::SProblem)}});
+      if (!rc) rc = plan_zero(p, G.counters, (size_t)ctrs * 4 + 16);
+      if (!rc) rc = plan_zero(p, G.next, 2 * sizeof(unsigned long long));
+      if (rc) { plan_free(p); return rc; }
     }
-    p->ns = (int)probs.size();
-    p->s_units = units;
-    void* buf;
-    int rc = plan_alloc(p, &buf, probs.size() * sizeof(grouped::SProblem));
-    if (!rc) { p->s_probs = static_cast<grouped::SProblem*>(buf); rc = plan_alloc(p, &buf, (size_t)parts * 4); }
-    if (!rc) { p->s_partials = static_cast<float*>(buf); rc = plan_alloc(p, &buf, (size_t)ctrs * 4 + 16); }
-    if (!rc) { p->s_counters = static_cast<unsigned*>(buf); rc = plan_alloc(p, &buf, 2 * sizeof(unsigned long long)); }
-    if (!rc) p->s_next = static_cast<unsigned long long*>(buf);
-    if (rc) { plan_free(p); return rc; }
-    const size_t off = p->host_tables.size();
-    rc = plan_upload(p, p->s_probs, probs.data(), probs.size() * sizeof(grouped::SProblem));
-    if (!rc && async) pending.push_back({p->s_probs, {off, probs.size() * sizeof(grouped::SProblem)}});
-    if (!rc) rc = plan_zero(p, p->s_counters, (size_t)ctrs * 4 + 16);
-    if (!rc) rc = plan_zero(p, p->s_next, 2 * sizeof(unsigned long long));
-    if (rc) { plan_free(p); return rc; }
   }
 
   // Ozaki problems with a data-chosen slice count: choose once now (one
@@ -592,16 +601,22 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     note_launch();
     if ((e = launch_status()) != cudaSuccess) return cuda_fail(e, "grouped f64 launch");
   }
-  if (p->ns) {
+  for (int t = 0; t < 2; ++t) {
+    const Plan::SGroup& G = p->sg[t];
+    if (!G.ns) continue;
     const int sms = (max_sms > 0 && max_sms < ds->sm_count) ? max_sms : ds->sm_count;
-    const int grid = (int)std::min<int64_t>(p->s_units, 2 * sms);
     KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
-    if (p->s_wide)
-      grouped::sgemm_grouped_kernel<uint64_t><<<grid, ffma::THREADS, ffma::SMEM_BYTES, s>>>(p->s_probs, p->ns, p->s_units,
-                                                                           p->s_next, p->s_partials, p->s_counters);
-    else
-      grouped::sgemm_grouped_kernel<uint32_t><<<grid, ffma::THREADS, ffma::SMEM_BYTES, s>>>(p->s_probs, p->ns, p->s_units,
-                                                                           p->s_next, p->s_partials, p->s_counters);
+    if (t == 1) {
+      using T = ffma::Tile<64>;
+      const int grid = (int)std::min<int64_t>(G.units, (int64_t)T::CTAS_PER_SM * sms);
+      auto k = G.wide ? grouped::sgemm_grouped_kernel<64, uint64_t> : grouped::sgemm_grouped_kernel<64, uint32_t>;
+      k<<<grid, T::THREADS, T::SMEM_BYTES, s>>>(G.probs, G.ns, G.units, G.next, G.partials, G.counters);
+    } else {
+      using T = ffma::Tile<128>;
+      const int grid = (int)std::min<int64_t>(G.units, (int64_t)T::CTAS_PER_SM * sms);
+      auto k = G.wide ? grouped::sgemm_grouped_kernel<128, uint64_t> : grouped::sgemm_grouped_kernel<128, uint32_t>;
+      k<<<grid, T::THREADS, T::SMEM_BYTES, s>>>(G.probs, G.ns, G.units, G.next, G.partials, G.counters);
+    }
     note_launch();
     if ((e = launch_status()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
   }

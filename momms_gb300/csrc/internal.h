@@ -243,10 +243,16 @@ int repack_colmajor(const DevMat& src, int64_t rows, int64_t cols, size_t elem, 
 // contiguous, 1 = TMA with k contiguous, 2 = needs a column-major repack.
 int dmma_orient(const DevMat& v, int64_t rows, int64_t cols, bool x_is_rows);
 
-// Split-k count of a plain f64 / f32 problem: from the tuning table
-// (momms_autotune) or the model. Depends only on the shape and the SM count.
+// Launch configuration of a plain f64 / f32 problem: the output tile
+// (0 = the kernel's 128 x 128 tile, 1 = its small tile: FFMA 64 x 64) and the
+// k-split count, from the tuning table (momms_autotune, keyed by shape
+// bucket) or the model. Depends only on the shape and the SM count.
+struct PlainCfg {
+  int tile;
+  int splits;
+};
+PlainCfg plain_cfg(int dtype, int64_t m, int64_t n, int64_t k, int sm_count);
 int splits_f64(int64_t m, int64_t n, int64_t k, int sm_count);
-int splits_f32(int64_t m, int64_t n, int64_t k, int sm_count);
 
 // Ozaki: choose the slice count for `d` from its target with the sampled
 // bound (synchronises `s`).

@@ -26,9 +26,11 @@ struct Params {
 
 // SPLIT: the launch splits k (p.sched.splits > 1); without it the unit loop
 // carries no split bookkeeping, which keeps the main loop within 128
-// registers (2 CTAs per SM) without spilling.
-template <bool A_XC, bool B_XC, typename Off, bool SPLIT>
-__global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const __grid_constant__ Params p) {
+// registers (2 CTAs of 256 threads, or 8 of 64, per SM) without spilling.
+// TM: the tile edge (128 or 64).
+template <int TM, bool A_XC, bool B_XC, typename Off, bool SPLIT>
+__global__ void __launch_bounds__(Tile<TM>::THREADS, Tile<TM>::CTAS_PER_SM)
+    sgemm_kernel(const __grid_constant__ Params p) {
   extern __shared__ float4 ffma_smem[];
   __shared__ int s_last;
   const Operands& o = p.o;
@@ -44,16 +46,32 @@ __global__ void __launch_bounds__(THREADS, 2) sgemm_kernel(const __grid_constant
     for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-    prefetch_c_tile(p.e, tm, tn);
-    ffma_unit_t<A_XC, B_XC, Off>(o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
+    prefetch_c_tile<TM>(p.e, tm, tn);
+    ffma_unit_t<TM, A_XC, B_XC, Off>(o, tm, tn, kb0, kb1, acc, reinterpret_cast<float*>(ffma_smem));
     if (SPLIT) {
       const int64_t tile = u / p.sched.splits;
-      ffma_finish(p.e, acc, tm, tn, p.sched.splits, sp, p.partials + (size_t)tile * p.sched.splits * BM * BN,
-                  p.counters + tile, &s_last);
+      ffma_finish<TM>(p.e, acc, tm, tn, p.sched.splits, sp, p.partials + (size_t)tile * p.sched.splits * TM * TM,
+                      p.counters + tile, &s_last);
     } else {
-      ffma_finish(p.e, acc, tm, tn, 1, 0, nullptr, nullptr, &s_last);
+      ffma_finish<TM>(p.e, acc, tm, tn, 1, 0, nullptr, nullptr, &s_last);
     }
   }
+}
+
+typedef void (*Kern)(const Params);
+// The instantiations of one tile size, by [A layout][B layout][offset width][split].
+template <int TM>
+const Kern (&kernel_table())[2][2][2][2] {
+  static const Kern t[2][2][2][2] = {
+      {{{sgemm_kernel<TM, false, false, uint32_t, false>, sgemm_kernel<TM, false, false, uint32_t, true>},
+        {sgemm_kernel<TM, false, false, uint64_t, false>, sgemm_kernel<TM, false, false, uint64_t, true>}},
+       {{sgemm_kernel<TM, false, true, uint32_t, false>, sgemm_kernel<TM, false, true, uint32_t, true>},
+        {sgemm_kernel<TM, false, true, uint64_t, false>, sgemm_kernel<TM, false, true, uint64_t, true>}}},
+      {{{sgemm_kernel<TM, true, false, uint32_t, false>, sgemm_kernel<TM, true, false, uint32_t, true>},
+        {sgemm_kernel<TM, true, false, uint64_t, false>, sgemm_kernel<TM, true, false, uint64_t, true>}},
+       {{sgemm_kernel<TM, true, true, uint32_t, false>, sgemm_kernel<TM, true, true, uint32_t, true>},
+        {sgemm_kernel<TM, true, true, uint64_t, false>, sgemm_kernel<TM, true, true, uint64_t, true>}}}};
+  return t;
 }
 
 }  // namespace ffma
@@ -98,11 +116,14 @@ int sgemm_ffma_impl(const DevGemm& g0, cudaStream_t s, void* (&scratch)[3]) {
   p.o = Operands{static_cast<const float*>(g.a.ptr), g.a.rs, g.a.cs, static_cast<const float*>(g.b.ptr), g.b.rs,
                  g.b.cs, g.m, g.n, g.k, a_xc, b_xc, vec};
   p.e = Epi{g.m, g.n, (float)g.alpha, (float)g.beta, static_cast<float*>(g.c.ptr), g.c.rs, g.c.cs};
-  const int tiles_m = (int)ceil_div(g.m, BM), tiles_n = (int)ceil_div(g.n, BN);
+  // the tile and split count of this shape (tuning table or model)
+  const PlainCfg cfg = plain_cfg(MOMMS_DTYPE_F32, g.m, g.n, g.k, ds->sm_count);
+  const int TMv = cfg.tile == 1 ? 64 : 128;
+  const int tiles_m = (int)ceil_div(g.m, TMv), tiles_n = (int)ceil_div(g.n, TMv);
   const int64_t tiles = (int64_t)tiles_m * tiles_n;
   const int64_t kblocks = ceil_div(g.k, BK);
-  const int slots = ds->sm_count * 2;
-  int splits = splits_f32(g.m, g.n, g.k, ds->sm_count);
+  const int slots = ds->sm_count * (cfg.tile == 1 ? Tile<64>::CTAS_PER_SM : Tile<128>::CTAS_PER_SM);
+  int splits = cfg.splits;
   int64_t kb_split = ceil_div(kblocks, splits);
   splits = (int)ceil_div(kblocks, kb_split);
   p.sched = TileSched{tiles_m, tiles_n, splits, 8, kb_split * BK};
@@ -111,7 +132,7 @@ int sgemm_ffma_impl(const DevGemm& g0, cudaStream_t s, void* (&scratch)[3]) {
   p.counters = nullptr;
   void*& ws = scratch[2];
   if (splits > 1) {
-    size_t part_bytes = (size_t)tiles * splits * BM * BN * 4;
+    size_t part_bytes = (size_t)tiles * splits * TMv * TMv * 4;
     size_t cnt_bytes = (size_t)tiles * 4;
     if ((ce = scratch_alloc(&ws, part_bytes + cnt_bytes, s)) != cudaSuccess) return cuda_fail(ce, "split-k workspace");
     p.partials = static_cast<float*>(ws);
@@ -121,19 +142,12 @@ int sgemm_ffma_impl(const DevGemm& g0, cudaStream_t s, void* (&scratch)[3]) {
   const int grid = (int)std::min<int64_t>(p.sched.units(), slots);
   {
     KernelTimer kt(MOMMS_KERNEL_SGEMM_FFMA, s);
-    // one instantiation per (A layout, B layout, offset width, split)
-    typedef void (*Kern)(const Params);
-    static const Kern table[2][2][2][2] = {
-        {{{sgemm_kernel<false, false, uint32_t, false>, sgemm_kernel<false, false, uint32_t, true>},
-          {sgemm_kernel<false, false, uint64_t, false>, sgemm_kernel<false, false, uint64_t, true>}},
-         {{sgemm_kernel<false, true, uint32_t, false>, sgemm_kernel<false, true, uint32_t, true>},
-          {sgemm_kernel<false, true, uint64_t, false>, sgemm_kernel<false, true, uint64_t, true>}}},
-        {{{sgemm_kernel<true, false, uint32_t, false>, sgemm_kernel<true, false, uint32_t, true>},
-          {sgemm_kernel<true, false, uint64_t, false>, sgemm_kernel<true, false, uint64_t, true>}},
-         {{sgemm_kernel<true, true, uint32_t, false>, sgemm_kernel<true, true, uint32_t, true>},
-          {sgemm_kernel<true, true, uint64_t, false>, sgemm_kernel<true, true, uint64_t, true>}}}};
-    const Kern k = table[a_xc][b_xc][offsets_fit_32(p.o) ? 0 : 1][splits > 1 ? 1 : 0];
-    k<<<grid, THREADS, SMEM_BYTES, s>>>(p);
+    // one instantiation per (tile, A layout, B layout, offset width, split)
+    const int li = offsets_fit_32(p.o) ? 0 : 1, si = splits > 1 ? 1 : 0;
+    if (cfg.tile == 1)
+      kernel_table<64>()[a_xc][b_xc][li][si]<<<grid, Tile<64>::THREADS, Tile<64>::SMEM_BYTES, s>>>(p);
+    else
+      kernel_table<128>()[a_xc][b_xc][li][si]<<<grid, Tile<128>::THREADS, Tile<128>::SMEM_BYTES, s>>>(p);
   }
   note_launch();
   ce = launch_status();

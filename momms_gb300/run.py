@@ -33,6 +33,7 @@ def main():
     p.add_argument("--kernels", action="store_true",
                    help="also report each kernel class's mean time per call (CUDA events per launch)")
     p.add_argument("--batched", type=int, default=0, help="time a plan of this many uneven problems instead")
+    p.add_argument("--tune", action="store_true", help="with --batched: autotune every shape bucket first")
     a = p.parse_args()
     if a.batched:
         return run_batched(a)
@@ -120,8 +121,25 @@ def run_batched(a):
         flops += 2.0 * m * n * k
     s = torch.cuda.current_stream()
     sp = ctypes.c_void_p(s.cuda_stream)
+    lib.momms_tune_clear()
+    tuned = ctypes.c_int32(0)
+    if a.tune:
+        mg.check(lib.momms_autotune_batch(descs, a.batched, sp, ctypes.byref(tuned)), lib)
     plan = ctypes.c_void_p()
     mg.check(lib.momms_plan_create(descs, a.batched, ctypes.byref(plan)), lib)
+    # per-kernel split from uncaptured launches
+    lib.momms_timing_enable(1)
+    for kc in (mg.KERNEL_DGEMM_DMMA, mg.KERNEL_SGEMM_FFMA):
+        lib.momms_timing_read(kc, None, None, 1)
+    for _ in range(max(1, a.reps)):
+        mg.check(lib.momms_plan_launch(plan, sp), lib)
+    split = {}
+    for kc, name in ((mg.KERNEL_DGEMM_DMMA, "f64_kernel_ms"), (mg.KERNEL_SGEMM_FFMA, "f32_kernel_ms")):
+        t = ctypes.c_double(0)
+        n_ = ctypes.c_ulonglong(0)
+        lib.momms_timing_read(kc, ctypes.byref(t), ctypes.byref(n_), 1)
+        split[name] = t.value / max(1, a.reps)
+    lib.momms_timing_enable(0)
     mg.check(lib.momms_plan_capture(plan, sp), lib)
     for _ in range(a.warmup):
         mg.check(lib.momms_plan_launch(plan, sp), lib)
@@ -133,9 +151,15 @@ def run_batched(a):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / max(1, a.reps)
     lib.momms_plan_destroy(plan)
-    print(json.dumps({"batched": a.batched, "f64_problems": int((kinds != 2).sum()),
-                      "f32_problems": int((kinds == 2).sum()), "ms": ms,
-                      "tflops": flops / (ms * 1e-3) / 1e12}))
+    f64_flops = sum(2.0 * float(dims[i][0] * dims[i][1] * dims[i][2]) for i in range(a.batched) if kinds[i] != 2)
+    out = {"batched": a.batched, "f64_problems": int((kinds != 2).sum()), "f32_problems": int((kinds == 2).sum()),
+           "ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "tuned_buckets": tuned.value, **split}
+    if split.get("f64_kernel_ms"):
+        out["f64_tflops"] = f64_flops / (split["f64_kernel_ms"] * 1e-3) / 1e12
+    if split.get("f32_kernel_ms"):
+        out["f32_tflops"] = (flops - f64_flops) / (split["f32_kernel_ms"] * 1e-3) / 1e12
+    lib.momms_tune_clear()
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

@@ -102,13 +102,22 @@ def test_last_error_message(lib):
 
 def test_tune_table_text_roundtrip(lib):
     lib.momms_tune_clear()
-    assert lib.momms_tune_import(b"0 0 100 200 300 4\n1 0 64 64 9000 8\n") == mg.OK
+    # entries are keyed by shape bucket (ceil(log2) of m, n, k) and exported
+    # as the bucket's largest shape; the tile field is optional on import
+    assert lib.momms_tune_import(b"0 0 100 200 300 4\n1 0 64 64 9000 8 1\n") == mg.OK
     need = ctypes.c_size_t(0)
     assert lib.momms_tune_export(None, 0, ctypes.byref(need)) == mg.OK
     buf = ctypes.create_string_buffer(need.value)
     assert lib.momms_tune_export(buf, need.value, None) == mg.OK
     rows = sorted(buf.value.decode().strip().split("\n"))
-    assert rows == ["0 0 100 200 300 4", "1 0 64 64 9000 8"]
+    assert rows == ["0 0 128 256 512 4 0", "1 0 64 64 16384 8 1"]
+    # a shape of the same bucket replaces the entry
+    assert lib.momms_tune_import(b"0 0 120 129 260 6") == mg.OK
+    assert lib.momms_tune_export(None, 0, ctypes.byref(need)) == mg.OK
+    buf = ctypes.create_string_buffer(need.value)
+    assert lib.momms_tune_export(buf, need.value, None) == mg.OK
+    assert "0 0 128 256 512 6 0" in buf.value.decode()
+    assert lib.momms_tune_import(b"0 0 8 8 8 4 1") == mg.ERR_INVALID_ARG  # f64 has one tile
     small = ctypes.create_string_buffer(4)
     assert lib.momms_tune_export(small, 4, None) == mg.ERR_INVALID_ARG
     assert lib.momms_tune_import(b"garbage") == mg.ERR_INVALID_ARG

@@ -132,7 +132,8 @@ def test_autotune_records_and_keeps_c(gpu):
     buf = ctypes.create_string_buffer(need.value)
     mg.check(gpu.momms_tune_export(buf, need.value, None), gpu)
     line = buf.value.decode().strip()
-    assert line == f"0 0 {m} {n} {k} {res.splits}"
+    # keyed by the shape's bucket, written as the bucket's largest shape
+    assert line == f"0 0 128 128 8192 {res.splits} {res.tile}"
     # the tuned plan is used and the result is still inside the bound
     mg.check(gpu.momms_gemm(ctypes.byref(d), None), gpu)
     torch.cuda.synchronize()
