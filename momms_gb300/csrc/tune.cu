@@ -9,9 +9,8 @@
 // scratch output) is keyed by shape bucket: ceil(log2) of m, n and k, so a
 // tuned shape covers every problem within a factor of two of it and a batch
 // of uneven problems hits tuned entries. Shapes without an entry use a model:
-// the small tile when the large tiles cannot fill the GPU's CTA slots, then
-// split k only while the tiles still leave slots idle, keeping at least 2
-// (f64, 32 of k) / 8 (f32, 128 of k) k-blocks per split.
+// the large tile, and k split only while the tiles leave CTA slots idle,
+// keeping at least 2 (f64, 32 of k) / 8 (f32, 128 of k) k-blocks per split.
 #include <stdio.h>
 #include <string.h>
 
@@ -87,17 +86,14 @@ PlainCfg plain_cfg(int dtype, int64_t m, int64_t n, int64_t k, int sm_count) {
     c.splits = clamp_splits(model_splits(tiles, kblocks, sm_count, 2), kblocks);
     return c;
   }
-  // f32: the 64 x 64 tile (eight CTAs per SM) when 128 x 128 tiles (two per
-  // SM) leave CTA slots idle
+  // f32: the 128 x 128 tile (two CTAs per SM), split while its tiles leave
+  // CTA slots idle. The 64 x 64 tile is chosen only by the tuner: as the
+  // model's choice for every shape whose large tiles leave slots idle it took
+  // the f32 part of the 512-problem batch from 0.65 to 0.85 ms (a second
+  // persistent launch per batch, and no faster per problem there).
   const int64_t tiles128 = ceil_div(m, 128) * ceil_div(n, 128);
-  if (tiles128 < 2 * (int64_t)sm_count) {
-    const int64_t tiles64 = ceil_div(m, 64) * ceil_div(n, 64);
-    c.tile = 1;
-    c.splits = clamp_splits(model_splits(tiles64, kblocks, 8 * (int64_t)sm_count, 8), kblocks);
-  } else {
-    c.tile = 0;
-    c.splits = 1;
-  }
+  c.tile = 0;
+  c.splits = clamp_splits(model_splits(tiles128, kblocks, 2 * (int64_t)sm_count, 8), kblocks);
   return c;
 }
 
