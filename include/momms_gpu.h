@@ -197,8 +197,11 @@ int momms_stream_plan(const momms_gemm_desc* desc, uint64_t budget, int64_t* mb,
 /* ---- Grouped launches and execution plans --------------------------------
  * Many independent GEMMs run as one persistent kernel per dtype: every plain
  * f64 problem's tiles (and k-splits) are work units of one DMMA kernel, every
- * plain f32 problem's of one FFMA kernel; Ozaki and split-TF32 problems run
- * their own kernel sequences after them. Each problem is planned from its own
+ * plain f32 problem's of one FFMA kernel per output tile size; the slice
+ * products of all emulated (Ozaki) problems with unpacked operands and k up to
+ * 32704 are work units of one tcgen05 kernel (each problem's digit planes are
+ * prepared and its recombination run by its own small kernels); split-TF32
+ * and other emulated problems run their own kernel sequences. Each problem is planned from its own
  * shape only (tile, split-k: the tuning table or the model), so a problem
  * gives bit-identical results alone (momms_gemm) and in any batch. Plans take
  * device operands only. The reference runs one composed algorithm per call

@@ -250,6 +250,8 @@ struct Plan {
   } sg[2];
   // problems run by their own launch sequence (Ozaki, split-TF32)
   std::vector<PlanProblem> other;
+  // two or more emulated problems with fixed slice counts: one slice launch
+  OzakiBatch* ozb = nullptr;
   // operands copied to column-major scratch before each launch (f64
   // operands whose strides do not suit TMA)
   struct Repack {
@@ -279,6 +281,7 @@ int plan_alloc(Plan* p, void** out, size_t bytes) {
 
 void plan_free(Plan* p) {
   if (p->graph) cudaGraphExecDestroy(p->graph);
+  ozaki_batch_destroy(p->ozb);
   for (void* a : p->allocs) {
     if (p->async) cudaFreeAsync(a, p->stream);
     else cudaFree(a);
@@ -567,6 +570,29 @@ int plan_create(const momms_gemm_desc* descs, int count, Plan** out, cudaStream_
       pp.slices = s;
     }
   }
+  // Emulated problems that qualify run together: their slice products in one
+  // persistent launch (ozaki_batch_*); the rest keep their own sequences.
+  {
+    std::vector<DevGemm> gs;
+    std::vector<int> sl;
+    std::vector<PlanProblem> rest;
+    for (PlanProblem& pp : p->other) {
+      const DevGemm g = devgemm_of(pp.d);
+      if (pp.d.precision == MOMMS_PREC_OZAKI && ozaki_batchable(g, pp.slices)) {
+        gs.push_back(g);
+        sl.push_back(pp.slices);
+      } else {
+        rest.push_back(pp);
+      }
+    }
+    int clusters = 0;
+    if (gs.size() >= 2 && sp_pairs_available(&clusters)) {
+      const int rc = ozaki_batch_create(gs.data(), sl.data(), (int)gs.size(), async ? async_stream : nullptr, async,
+                                        &p->ozb);
+      if (rc) { plan_free(p); return rc; }
+      p->other = rest;
+    }
+  }
   // stream-ordered uploads: the host copies live in p->host_tables (no more
   // appends from here on, so the addresses are stable)
   for (auto& pu : pending) {
@@ -619,6 +645,10 @@ int plan_launch(Plan* p, cudaStream_t s, int max_sms) {
     }
     note_launch();
     if ((e = launch_status()) != cudaSuccess) return cuda_fail(e, "grouped f32 launch");
+  }
+  if (p->ozb) {
+    const int rc = ozaki_batch_launch(p->ozb, s, max_sms);
+    if (rc) return rc;
   }
   for (PlanProblem& pp : p->other) {
     const DevGemm g = devgemm_of(pp.d);

@@ -254,7 +254,21 @@ struct PlainCfg {
 PlainCfg plain_cfg(int dtype, int64_t m, int64_t n, int64_t k, int sm_count);
 int splits_f64(int64_t m, int64_t n, int64_t k, int sm_count);
 
-// Ozaki: choose the slice count for `d` from its target with the sampled
+// Emulated problems of a plan run together: each problem's preparation and
+// recombination, and ONE persistent slice-kernel launch (CTA pairs) over all
+// of their tiles, from a device table of their schedules and tensor maps.
+// Buffers and tables are made once at creation (`async`: stream-ordered on
+// `s`, which is synchronised once for the table uploads). A problem qualifies
+// with a fixed slice count, unpacked operands and k within one launch.
+struct OzakiBatch;
+bool ozaki_batchable(const DevGemm& g, int slices);
+// True when this device can run the CTA-pair slice kernel (*clusters: pairs at once).
+bool sp_pairs_available(int* clusters);
+int ozaki_batch_create(const DevGemm* gs, const int* slices, int count, cudaStream_t s, bool async, OzakiBatch** out);
+int ozaki_batch_launch(OzakiBatch* b, cudaStream_t s, int max_sms);
+void ozaki_batch_destroy(OzakiBatch* b);
+
+// Ozaki: choose the slice count for `d` from its target with the guaranteed
 // bound (synchronises `s`).
 int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s);
 

@@ -34,6 +34,7 @@
 #include <type_traits>
 
 #include "internal.h"
+#include "exact_round.cuh"
 #include "planes.cuh"
 #include "slicegemm.cuh"
 
@@ -363,6 +364,8 @@ struct CombineParams {
   uint8_t gb[sp::MAX_GROUPS];  // left shift within the word
   int scale_off;  // -2 bits - bits*dmax
   int alpha_one, beta_zero;
+  int wide;  // some group has word 3 (13-15 slices): R may pass 2^127 (wide_to_double)
+  int levels;  // > 0: group g has weight 2^(bits g) for g < levels = ng (combine_kernel's fixed form)
   int64_t m;
   int64_t j0, j1;  // columns of C this launch finishes
   const int* row_exp;
@@ -372,77 +375,37 @@ struct CombineParams {
   int64_t rsc, csc;
 };
 
-// Nearest double to a 128-bit signed integer times 2^scale.
-__device__ __forceinline__ double i128_to_double(__int128 R, int scale) {
-  if (R == 0) return 0.0;
-  const bool neg = R < 0;
-  unsigned __int128 U = neg ? (unsigned __int128)(-R) : (unsigned __int128)R;
-  const unsigned long long hi = (unsigned long long)(U >> 64);
-  unsigned long long top;
-  int sh = 0;
-  if (hi == 0) {
-    top = (unsigned long long)U;
-  } else {
-    sh = 64 - __clzll((long long)hi);  // significant bits above the low word
-    top = (unsigned long long)(U >> sh);
-    const unsigned __int128 rest = U & (((unsigned __int128)1 << sh) - 1);
-    if (rest != 0) top |= 1ull;  // sticky bit: top keeps 64 significant bits
-  }
-  // Round top to 53 significant bits (nearest, ties to even) and place the
-  // exponent directly: integer instructions only, since GB300's FP64 pipe is
-  // narrow. Same result as converting top to double (the only rounding) and
-  // scaling by 2^(sh + scale) exactly, which is what the rare results outside
-  // the normal range still do.
-  const int lz = __clzll((long long)top);
-  const unsigned long long t = top << lz;  // bit 63 set
-  unsigned long long mant = t >> 11;
-  const unsigned rb = (unsigned)(t & 0x7ffull);
-  if (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ++mant;
-  int E = 63 - lz + sh + scale;  // value = (mant / 2^52) * 2^E
-  if (mant >> 53) {
-    mant >>= 1;
-    ++E;
-  }
-  if (E < -1022 || E > 1023) {
-    const double v = __ull2double_rn(top);
-    return ldexp(neg ? -v : v, sh + scale);
-  }
-  const unsigned long long b = ((unsigned long long)(E + 1023) << 52) | (mant & ((1ull << 52) - 1)) |
-                               (neg ? (1ull << 63) : 0ull);
-  return __longlong_as_double((long long)b);
-}
-
-// Nearest double to R * 2^scale, R = P0 + P1 2^32 + P2 2^64 + P3 2^96 exactly
-// (|R| < 2^148). R below 2^126 in magnitude goes through i128_to_double as
-// is; a wider R is first shifted right to 126 bits with the lost bits kept
-// as a sticky bit 0 (more than the 53 + 2 bits the rounding looks at), which
-// leaves the rounded result unchanged.
-__device__ __forceinline__ double wide_to_double(long long P0, long long P1, long long P2, long long P3, int scale) {
-  const __int128 low = (__int128)P0 + ((__int128)P1 << 32);        // |.| < 2^93
-  const __int128 hi = (__int128)P2 + ((__int128)P3 << 32) + (low >> 64);  // R = hi 2^64 + lo, lo in [0, 2^64)
-  const unsigned long long lo = (unsigned long long)low;
-  const __int128 lim = (__int128)1 << 61;
-  if (hi >= -lim && hi < lim) return i128_to_double((__int128)(((unsigned __int128)hi << 64) | lo), scale);
-  const bool neg = hi < 0;
-  // the magnitude as uh 2^64 + ul
-  unsigned __int128 uh = neg ? (unsigned __int128)(-hi) - (lo != 0 ? 1u : 0u) : (unsigned __int128)hi;
-  const unsigned long long ul = neg ? (0ull - lo) : lo;
-  const unsigned long long uh_hi = (unsigned long long)(uh >> 64), uh_lo = (unsigned long long)uh;
-  const int nbh = uh_hi ? 128 - __clzll((long long)uh_hi) : 64 - __clzll((long long)uh_lo);  // bits of uh (>= 62)
-  const int s = nbh + 64 - 126;  // 1..22: the magnitude has nbh + 64 bits
-  unsigned __int128 u = (uh << (64 - s)) | (unsigned __int128)(ul >> s);
-  if (ul & ((1ull << s) - 1)) u |= 1u;  // sticky
-  return i128_to_double(neg ? -(__int128)u : (__int128)u, scale + s);
+// signed 32 x 32 -> 64-bit product plus c, one instruction
+__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
+  long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
 }
 
 // Thread rows i and i + 256 of block row blockIdx.x, for columns
 // j0 + blockIdx.y, stepping by gridDim.y: no index division, the row
 // exponents stay in registers, and the two rows' loads are in flight together.
-constexpr int kCombineBatch = 16;  // Horner entries whose loads are issued together
-
-__global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ CombineParams p) {
-  constexpr int bits = kDigitBits;
+//
+// The forms, one integer R:
+//  * NS > 0: one group per level (every k up to 8192), so group g's weight
+//    is 2^(bits g) and every word offset and shift is a compile-time
+//    constant: one 32 x 32 + 64-bit multiply-add per group and row;
+//  * NS == 0: any grouping, the weights read per group;
+//  * WIDE: 13-15 slices (a fourth partial sum and the conversion from up to
+//    148 bits), NARROW up to 12.
+// The kernel is bound by its issue rate and its memory latency together, so
+// the narrow forms keep to 64 registers (four blocks per SM). At 4096 x 4096
+// x 64 with 7 slices the runtime-weight form issued 332 instructions per
+// entry (ALU pipe 48 %, DRAM 30 % of peak, 298 us); the fixed form with
+// shift-and-add sums 194 (ALU 70 %, DRAM 65 %, 140 us).
+template <bool WIDE, int NS>
+__global__ void __launch_bounds__(256, WIDE ? 2 : 4) combine_kernel(const __grid_constant__ CombineParams p) {
+  static_assert(NS == 0 || (NS * kDigitBits <= 96) != WIDE, "the wide form is for levels past word 2");
   using u128 = unsigned __int128;
+  constexpr int NW = WIDE ? 4 : 3;
+  // group sums whose loads are issued together: NS, else every group of up
+  // to 8 (narrow) or 16 (wide) groups
+  constexpr int kBatch = NS > 0 ? NS : (WIDE ? 16 : 8);
   int64_t rows[2], roff[2];
   int er[2];
 #pragma unroll
@@ -456,39 +419,52 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
   for (int64_t j = p.j0 + blockIdx.y; j < p.j1; j += gridDim.y) {
     const int ec = p.col_exp[j];
     const int* col = p.sbuf + (j / sp::BN) * (p.mpad * sp::BN) + (j % sp::BN) * sp::BM;
-    // C's old values are loaded with the group sums, not after the Horner
-    // steps, so a column costs one memory round trip
+    // C's old values are loaded with the group sums, not after the sums, so
+    // a column costs one memory round trip
     double c_old[2] = {0.0, 0.0};
     if (!p.beta_zero) {
       c_old[0] = p.c[rows[0] * p.rsc + j * p.csc];
       if (two) c_old[1] = p.c[rows[1] * p.rsc + j * p.csc];
     }
-    // the four 64-bit partial sums of each of the two rows (see CombineParams)
-    long long P0[2] = {0, 0}, P1[2] = {0, 0}, P2[2] = {0, 0}, P3[2] = {0, 0};
-    auto add = [&](int u, int s_g, int g) {
-      const int w = p.gw[g];
-      const long long t = (long long)s_g << p.gb[g];
-      if (w == 0) P0[u] += t;
-      else if (w == 1) P1[u] += t;
-      else if (w == 2) P2[u] += t;
-      else P3[u] += t;
-    };
-    if (p.ng <= kCombineBatch) {
-      // all loads first (up to 2 x kCombineBatch in flight), then the sums
-      int s0[kCombineBatch], s1[kCombineBatch];
+    // the 64-bit partial sums of each of the two rows (see CombineParams)
+    long long P[NW][2];
 #pragma unroll
-      for (int q = 0; q < kCombineBatch; ++q) {
+    for (int w = 0; w < NW; ++w) P[w][0] = P[w][1] = 0;
+    auto add = [&](int u, int s_g, int g) {
+      const int w = p.gw[g], f = 1 << p.gb[g];  // gb <= 24
+      if (w == 0) {
+        P[0][u] = mad_wide(s_g, f, P[0][u]);
+      } else if (w == 1) {
+        P[1][u] = mad_wide(s_g, f, P[1][u]);
+      } else if constexpr (WIDE) {
+        if (w == 2) P[2][u] = mad_wide(s_g, f, P[2][u]);
+        else P[NW - 1][u] = mad_wide(s_g, f, P[NW - 1][u]);
+      } else {
+        P[2][u] = mad_wide(s_g, f, P[2][u]);
+      }
+    };
+    if (NS > 0 || p.ng <= kBatch) {
+      // all loads first (up to 2 x kBatch in flight), then the sums
+      int s0[kBatch], s1[kBatch];
+#pragma unroll
+      for (int q = 0; q < kBatch; ++q) {
         s0[q] = 0;
         s1[q] = 0;
-        if (q < p.ng) {
+        if (NS > 0 || q < p.ng) {
           const int* sg = col + (int64_t)q * p.plane;
           s0[q] = sg[roff[0]];
           if (two) s1[q] = sg[roff[1]];
         }
       }
 #pragma unroll
-      for (int q = 0; q < kCombineBatch; ++q) {
-        if (q < p.ng) {
+      for (int q = 0; q < kBatch; ++q) {
+        if constexpr (NS > 0) {
+          // weight 2^(bits q): word (bits q) / 32, shift (bits q) % 32, both
+          // constants once the loop is unrolled
+          constexpr int bits = kDigitBits;
+          P[(bits * q) >> 5][0] = mad_wide(s0[q], 1 << ((bits * q) & 31), P[(bits * q) >> 5][0]);
+          P[(bits * q) >> 5][1] = mad_wide(s1[q], 1 << ((bits * q) & 31), P[(bits * q) >> 5][1]);
+        } else if (q < p.ng) {
           add(0, s0[q], q);
           add(1, s1[q], q);
         }
@@ -504,8 +480,16 @@ __global__ void __launch_bounds__(256) combine_kernel(const __grid_constant__ Co
     for (int u = 0; u < 2; ++u) {
       if (u == 1 && !two) break;
       double v;
-      if (er[u] == INT32_MAX || ec == INT32_MAX) v = __longlong_as_double(0x7ff8000000000000ll);
-      else v = wide_to_double(P0[u], P1[u], P2[u], P3[u], er[u] + ec + p.scale_off);
+      const int sc = er[u] + ec + p.scale_off;
+      if (er[u] == INT32_MAX || ec == INT32_MAX) {
+        v = __longlong_as_double(0x7ff8000000000000ll);
+      } else if constexpr (WIDE) {
+        v = wide_to_double(P[0][u], P[1][u], P[2][u], P[NW - 1][u], sc);
+      } else {
+        // |R| < 2^127: 128-bit two's complement holds it
+        const u128 R = (u128)(__int128)P[0][u] + ((u128)(__int128)P[1][u] << 32) + ((u128)(__int128)P[2][u] << 64);
+        v = i128_to_double((__int128)R, sc);
+      }
       double* cp = p.c + rows[u] * p.rsc + j * p.csc;
       const double sv = p.alpha_one ? v : v * p.alpha;  // v * 1 == v: one FP64 operation saved
       *cp = p.beta_zero ? sv : fma(p.beta, c_old[u], sv);
@@ -647,6 +631,99 @@ bool ozaki_schedule(int ns, int64_t k, Schedule* sc) {
   }
   sc->group_begin[sc->ng] = sc->np;
   return true;
+}
+}  // namespace
+
+namespace {
+// The slice kernel's parameters of an ns-slice product over k (rows m): the
+// schedule's pairs and groups, the TMEM chunk rule. Sizes along n, the output
+// planes and the status word are the caller's.
+bool slice_params(int ns, int64_t m, int64_t k, sp::Params* p, Schedule* sch) {
+  if (!ozaki_schedule(ns, k, sch)) return false;
+  memset(p, 0, sizeof(*p));
+  p->m = m;
+  p->kelems = 64;
+  p->kblocks = (int)ceil_div(k, 64);
+  p->tiles_m = (int)ceil_div(m, sp::BM);
+  const int np = sch->np, ng = sch->ng;
+  memcpy(p->pair_a, sch->pair_a, (size_t)np);
+  memcpy(p->pair_b, sch->pair_b, (size_t)np);
+  memcpy(p->group_begin, sch->group_begin, sizeof(int) * (size_t)(ng + 1));
+  memcpy(p->pair_w, sch->pair_w, sizeof(int) * (size_t)np);
+  p->chunk_cap = kChunkCap;
+  p->merge_pairs = 1;
+  p->ngroups = ng;
+  return true;
+}
+
+// The recombination's parameters for the whole of C (columns 0..n).
+void combine_params(const DevGemm& g, int ns, const Schedule& sch, const int* sbuf, int64_t plane, int64_t mpad,
+                    const int* rexp, const int* cexp, CombineParams* cp) {
+  const int bits = kDigitBits;
+  memset(cp, 0, sizeof(*cp));
+  cp->sbuf = sbuf;
+  cp->plane = plane;
+  cp->mpad = mpad;
+  // each group's weight 2^(bits*(dmax - level)) as (word, shift)
+  const int dmax = ns - 1;
+  cp->ng = sch.ng;
+  for (int gi = 0; gi < sch.ng; ++gi) {
+    const int sh = bits * (dmax - sch.level[gi]);
+    cp->gw[gi] = (uint8_t)(sh >> 5);
+    cp->gb[gi] = (uint8_t)(sh & 31);
+    if (cp->gw[gi] == 3) cp->wide = 1;
+  }
+  // one group per level, lowest first: the weights are 2^(bits g)
+  bool one_per_level = sch.ng <= kOzakiMaxSlices;
+  for (int gi = 0; gi < sch.ng && one_per_level; ++gi) one_per_level = 32 * cp->gw[gi] + cp->gb[gi] == bits * gi;
+  cp->levels = one_per_level ? sch.ng : 0;
+  cp->scale_off = -2 * bits - bits * dmax;
+  cp->alpha_one = (g.alpha == 1.0);
+  cp->beta_zero = (g.beta == 0.0);
+  cp->m = g.m;
+  cp->j0 = 0;
+  cp->j1 = g.n;
+  cp->row_exp = rexp;
+  cp->col_exp = cexp;
+  cp->alpha = g.alpha;
+  cp->beta = g.beta;
+  cp->c = static_cast<double*>(g.c.ptr);
+  cp->rsc = g.c.rs;
+  cp->csc = g.c.cs;
+}
+
+// One recombination launch over columns [j0, j1) of C on stream Y.
+int launch_combine(CombineParams cp, int64_t j0, int64_t j1, int sm_count, cudaStream_t Y) {
+  cp.j0 = j0;
+  cp.j1 = j1;
+  const int64_t bx = ceil_div(cp.m, 512);
+  const int64_t by = std::min<int64_t>({j1 - j0, 65535, std::max<int64_t>(1, (int64_t)sm_count * 16 / bx)});
+  {
+    KernelTimer kt(MOMMS_KERNEL_COMBINE, Y);
+    const dim3 grid((unsigned)bx, (unsigned)by);
+    switch (cp.levels ? cp.levels : (cp.wide ? -1 : 0)) {
+      case -1: combine_kernel<true, 0><<<grid, 256, 0, Y>>>(cp); break;
+      case 13: combine_kernel<true, 13><<<grid, 256, 0, Y>>>(cp); break;
+      case 14: combine_kernel<true, 14><<<grid, 256, 0, Y>>>(cp); break;
+      case 15: combine_kernel<true, 15><<<grid, 256, 0, Y>>>(cp); break;
+      case 1: combine_kernel<false, 1><<<grid, 256, 0, Y>>>(cp); break;
+      case 2: combine_kernel<false, 2><<<grid, 256, 0, Y>>>(cp); break;
+      case 3: combine_kernel<false, 3><<<grid, 256, 0, Y>>>(cp); break;
+      case 4: combine_kernel<false, 4><<<grid, 256, 0, Y>>>(cp); break;
+      case 5: combine_kernel<false, 5><<<grid, 256, 0, Y>>>(cp); break;
+      case 6: combine_kernel<false, 6><<<grid, 256, 0, Y>>>(cp); break;
+      case 7: combine_kernel<false, 7><<<grid, 256, 0, Y>>>(cp); break;
+      case 8: combine_kernel<false, 8><<<grid, 256, 0, Y>>>(cp); break;
+      case 9: combine_kernel<false, 9><<<grid, 256, 0, Y>>>(cp); break;
+      case 10: combine_kernel<false, 10><<<grid, 256, 0, Y>>>(cp); break;
+      case 11: combine_kernel<false, 11><<<grid, 256, 0, Y>>>(cp); break;
+      case 12: combine_kernel<false, 12><<<grid, 256, 0, Y>>>(cp); break;
+      default: combine_kernel<false, 0><<<grid, 256, 0, Y>>>(cp); break;
+    }
+  }
+  note_launch();
+  const cudaError_t e = launch_status();
+  return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "Ozaki launch");
 }
 }  // namespace
 
@@ -1168,24 +1245,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   }
 
   sp::Params p;
-  memset(&p, 0, sizeof(p));
-  p.m = m;
-  p.kelems = 64;
-  p.kblocks = (int)ceil_div(k, 64);
-  p.tiles_m = (int)ceil_div(m, sp::BM);
-  CombineParams cp;
-  memset(&cp, 0, sizeof(cp));
   Schedule sch;
-  if (!ozaki_schedule(ns, k, &sch)) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
+  if (!slice_params(ns, m, k, &p, &sch)) return fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
   const int np = sch.np, ng = sch.ng;
-  const uint8_t* dgrp = sch.level;
-  memcpy(p.pair_a, sch.pair_a, (size_t)np);
-  memcpy(p.pair_b, sch.pair_b, (size_t)np);
-  memcpy(p.group_begin, sch.group_begin, sizeof(int) * (size_t)(ng + 1));
-  memcpy(p.pair_w, sch.pair_w, sizeof(int) * (size_t)np);
-  p.chunk_cap = kChunkCap;
-  p.merge_pairs = 1;
-  p.ngroups = ng;
   call_info().slices = ns;
   call_info().pairs = np;
   call_info().groups = ng;
@@ -1200,31 +1262,8 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
   ScratchGuard free_sbuf(sbuf, s);
   p.plane = (int64_t)plane;
   p.status = ds->status;
-
-  cp.sbuf = sbuf;
-  cp.plane = (int64_t)plane;
-  cp.mpad = mpad;
-  {
-    // each group's weight 2^(bits*(dmax - level)) as (word, shift)
-    const int dmax = ns - 1;
-    cp.ng = ng;
-    for (int gi = 0; gi < ng; ++gi) {
-      const int sh = bits * (dmax - dgrp[gi]);
-      cp.gw[gi] = (uint8_t)(sh >> 5);
-      cp.gb[gi] = (uint8_t)(sh & 31);
-    }
-    cp.scale_off = -2 * bits - bits * dmax;
-    cp.alpha_one = (g.alpha == 1.0);
-    cp.beta_zero = (g.beta == 0.0);
-  }
-  cp.m = m;
-  cp.row_exp = rexp;
-  cp.col_exp = cexp;
-  cp.alpha = g.alpha;
-  cp.beta = g.beta;
-  cp.c = static_cast<double*>(g.c.ptr);
-  cp.rsc = g.c.rs;
-  cp.csc = g.c.cs;
+  CombineParams cp;
+  combine_params(g, ns, sch, sbuf, (int64_t)plane, mpad, rexp, cexp, &cp);
 
   // The second stream starts after everything above (scratch, A, the
   // choice), and so does the verify stream V, which runs the bound kernel
@@ -1249,19 +1288,9 @@ int launch_dgemm_ozaki(const DevGemm& g, double target, int slices, int* slices_
     if (e != cudaSuccess) return cuda_fail(e, "operand staging");
     const int64_t nsub = (nch == 1 && stg && stg->writeback) ? std::min<int64_t>(4, w) : 1;
     for (int64_t q = 0; q < nsub; ++q) {
-      cp.j0 = j0 + w * q / nsub;
-      cp.j1 = j0 + w * (q + 1) / nsub;
-      const int64_t bx = ceil_div(m, 512);
-      const int64_t by =
-          std::min<int64_t>({cp.j1 - cp.j0, 65535, std::max<int64_t>(1, (int64_t)ds->sm_count * 16 / bx)});
-      {
-        KernelTimer kt(MOMMS_KERNEL_COMBINE, Y);
-        combine_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, Y>>>(cp);
-      }
-      note_launch();
-      e = launch_status();
-      if (e != cudaSuccess) return cuda_fail(e, "Ozaki launch");
-      const int r2 = columns_done(g, cp.j0, cp.j1, Y);
+      const int64_t c0 = j0 + w * q / nsub, c1 = j0 + w * (q + 1) / nsub;
+      int r2 = launch_combine(cp, c0, c1, ds->sm_count, Y);
+      if (!r2) r2 = columns_done(g, c0, c1, Y);
       if (r2) return r2;
     }
     return MOMMS_OK;
@@ -1465,6 +1494,196 @@ int ozaki_choose_slices(const momms_gemm_desc& d, int* slices, cudaStream_t s) {
                 "Ozaki: the requested error %.3g cannot be guaranteed for every entry with 15 slices (pass a fixed "
                 "slice count to run anyway)",
                 target_or_fp64(d.target_rel_err));
+  return MOMMS_OK;
+}
+
+}  // namespace momms
+
+// ---------------------------------------------------------------------------
+// Emulated problems of a plan in one slice launch (OzakiBatch).
+// ---------------------------------------------------------------------------
+namespace momms {
+
+struct OzakiBatch {
+  struct Prob {
+    DevGemm g;
+    int ns = 0;
+    void* mem = nullptr;  // maxbits [m+n] u64, exps [m+n] int, planes, group sums
+    unsigned long long* maxbits = nullptr;
+    int* exps = nullptr;
+    __half* planes = nullptr;
+    int* sbuf = nullptr;
+    int64_t kp = 0;
+    size_t a_plane = 0, b_plane = 0;
+    CombineParams cp;
+  };
+  std::vector<Prob> probs;
+  sp::Params* d_params = nullptr;  // device problem table
+  CUtensorMap* d_maps = nullptr;   // [2 * count], A and B half-tile maps
+  int64_t units = 0;
+  bool async = false;
+  cudaStream_t stream = nullptr;
+};
+
+bool sp_pairs_available(int* clusters) {
+  return sp::slice_variant<0, sp::EPI_OZAKI>(clusters) == sp::SLICE_PAIR && *clusters > 0;
+}
+
+bool ozaki_batchable(const DevGemm& g, int slices) {
+  return slices > 0 && slices <= kOzakiMaxSlices && !g.pk[0] && !g.pk[1] && g.k <= kMaxK && g.m > 0 && g.n > 0 &&
+         g.k > 0;
+}
+
+void ozaki_batch_destroy(OzakiBatch* b) {
+  if (!b) return;
+  auto release = [&](void* p) {
+    if (!p) return;
+    if (b->async) cudaFreeAsync(p, b->stream);
+    else cudaFree(p);
+  };
+  for (auto& pr : b->probs) release(pr.mem);
+  release(b->d_params);
+  release(b->d_maps);
+  delete b;
+}
+
+int ozaki_batch_create(const DevGemm* gs, const int* slices, int count, cudaStream_t s, bool async, OzakiBatch** out) {
+  *out = nullptr;
+  DeviceState* ds = device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  OzakiBatch* b = new OzakiBatch();
+  b->async = async;
+  b->stream = s;
+  auto alloc = [&](void** p, size_t bytes) {
+    const cudaError_t e = async ? scratch_alloc_raw(p, bytes, s) : device_malloc(p, bytes);
+    return e == cudaSuccess ? MOMMS_OK : cuda_fail(e, "Ozaki batch allocation");
+  };
+  std::vector<sp::Params> params((size_t)count);
+  std::vector<CUtensorMap> maps((size_t)count * 2);
+  // problems ordered by falling cost (pairs x k-blocks x pair tiles), so the
+  // kernel hands out the largest units first
+  std::vector<int> order((size_t)count);
+  std::vector<double> cost((size_t)count);
+  for (int i = 0; i < count; ++i) {
+    order[(size_t)i] = i;
+    const DevGemm& g = gs[i];
+    cost[(size_t)i] = (double)ceil_div(g.m, 2 * sp::BM) * ceil_div(g.n, sp::BN) * ceil_div(g.k, 64) * slices[i] *
+                      (slices[i] + 1);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[(size_t)x] > cost[(size_t)y]; });
+  int rc = MOMMS_OK;
+  b->probs.resize((size_t)count);
+  for (int oi = 0; oi < count && !rc; ++oi) {
+    const int i = order[(size_t)oi];
+    OzakiBatch::Prob& P = b->probs[(size_t)oi];
+    P.g = gs[i];
+    P.ns = slices[i];
+    const int64_t m = P.g.m, n = P.g.n, k = P.g.k;
+    sp::Params& prm = params[(size_t)oi];
+    Schedule sch;
+    if (!slice_params(P.ns, m, k, &prm, &sch)) {
+      rc = fail(MOMMS_ERR_UNSUPPORTED, "Ozaki schedule needs too many groups");
+      break;
+    }
+    P.kp = round_up(k, 8);
+    P.a_plane = (size_t)m * P.kp;
+    P.b_plane = (size_t)n * P.kp;
+    const int64_t mpad = round_up(m, (int64_t)sp::BM);
+    const size_t plane = (size_t)mpad * (size_t)round_up(n, (int64_t)sp::BN);
+    const size_t eb = (size_t)round_up((m + n) * 12, 256);
+    const size_t pb = (size_t)round_up((int64_t)(P.ns * (P.a_plane + P.b_plane) * 2), 256);
+    rc = alloc(&P.mem, eb + pb + (size_t)sch.ng * plane * 4);
+    if (rc) break;
+    char* base = static_cast<char*>(P.mem);
+    P.maxbits = reinterpret_cast<unsigned long long*>(base);
+    P.exps = reinterpret_cast<int*>(P.maxbits + (m + n));
+    P.planes = reinterpret_cast<__half*>(base + eb);
+    P.sbuf = reinterpret_cast<int*>(base + eb + pb);
+    prm.n = n;
+    prm.tiles_n = (int)ceil_div(n, sp::BN);
+    prm.sbuf = P.sbuf;
+    prm.plane = (int64_t)plane;
+    prm.gchunk = prm.ngroups;  // a batch fills the GPU without splitting a tile's groups
+    prm.status = ds->status;
+    if (!sp::plan_chunks(prm)) {
+      rc = fail(MOMMS_ERR_UNSUPPORTED, "Ozaki chunk plan");
+      break;
+    }
+    prm.unit_begin = b->units;
+    b->units += (int64_t)((prm.tiles_m + 1) / 2) * prm.tiles_n;
+    combine_params(P.g, P.ns, sch, P.sbuf, (int64_t)plane, mpad, P.exps, P.exps + m, &P.cp);
+    // A [ns][m][kp] and B [ns][n][kp], 128-byte k-blocks, each CTA of a pair
+    // staging half of the 256-row B tile
+    uint64_t dims[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)P.ns};
+    uint64_t strides[2] = {(uint64_t)P.kp * 2, (uint64_t)P.a_plane * 2};
+    uint32_t box[3] = {64, (uint32_t)sp::BM, 1};
+    rc = encode_tiled(&maps[2 * (size_t)oi], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, P.planes, dims, strides, box,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) break;
+    uint64_t dimsb[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)P.ns};
+    uint64_t stridesb[2] = {(uint64_t)P.kp * 2, (uint64_t)P.b_plane * 2};
+    uint32_t boxh[3] = {64, (uint32_t)(sp::BN / 2), 1};
+    rc = encode_tiled(&maps[2 * (size_t)oi + 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, P.planes + P.ns * P.a_plane,
+                      dimsb, stridesb, boxh, CU_TENSOR_MAP_SWIZZLE_128B);
+  }
+  if (!rc) rc = alloc(reinterpret_cast<void**>(&b->d_params), params.size() * sizeof(sp::Params));
+  if (!rc) rc = alloc(reinterpret_cast<void**>(&b->d_maps), maps.size() * sizeof(CUtensorMap));
+  if (!rc) {
+    // synchronous uploads: the host tables need not outlive this call
+    cudaError_t e = cudaMemcpyAsync(b->d_params, params.data(), params.size() * sizeof(sp::Params),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "Ozaki batch tables");
+  }
+  if (rc) {
+    ozaki_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return MOMMS_OK;
+}
+
+int ozaki_batch_launch(OzakiBatch* b, cudaStream_t s, int max_sms) {
+  DeviceState* ds = device_state();
+  if (!ds) return MOMMS_ERR_NO_DEVICE;
+  if (b->probs.empty()) return MOMMS_OK;
+  // each problem's exponents and digit planes
+  for (auto& P : b->probs) {
+    const DevGemm& g = P.g;
+    const double* A = static_cast<const double*>(g.a.ptr);
+    const double* B = static_cast<const double*>(g.b.ptr);
+    int rc = ozaki_operand_exponents(A, g.a.rs, g.a.cs, g.m, g.k, P.maxbits, P.exps, s);
+    if (!rc) rc = ozaki_operand_exponents(B, g.b.cs, g.b.rs, g.n, g.k, P.maxbits + g.m, P.exps + g.m, s);
+    if (rc) return rc;
+    ozaki_operand_planes(P.ns, A, g.a.rs, g.a.cs, g.m, g.k, P.planes, P.kp, P.exps, s);
+    ozaki_operand_planes(P.ns, B, g.b.cs, g.b.rs, g.n, g.k, P.planes + P.ns * P.a_plane, P.kp, P.exps + g.m, s);
+  }
+  // one persistent slice launch over every problem's tiles
+  int clusters = 0;
+  if (sp::slice_variant<0, sp::EPI_OZAKI>(&clusters) != sp::SLICE_PAIR || clusters <= 0)
+    return fail(MOMMS_ERR_UNSUPPORTED, "grouped emulated launches need CTA pairs on this device");
+  if (max_sms > 0) clusters = std::max(1, std::min(clusters, max_sms / 2));
+  sp::GroupTable gt{b->d_params, b->d_maps, (int)b->probs.size(), b->units};
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = sp::cluster2_config(sp::P_SMEM_BYTES, attr);
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(b->units, clusters)));
+  cfg.stream = s;
+  cudaError_t e;
+  {
+    KernelTimer kt(MOMMS_KERNEL_SLICE_OZAKI, s);
+    const CUtensorMap unused{};
+    e = cudaLaunchKernelEx(&cfg, sp::slice_gemm_pair_kernel<0, sp::EPI_OZAKI, true>, unused, unused, sp::Params{},
+                           gt);
+    if (e == cudaSuccess) e = launch_status();
+  }
+  note_launch();
+  if (e != cudaSuccess) return cuda_fail(e, "grouped Ozaki slice launch");
+  for (auto& P : b->probs) {
+    const int rc = launch_combine(P.cp, 0, P.g.n, ds->sm_count, s);
+    if (rc) return rc;
+  }
   return MOMMS_OK;
 }
 

@@ -106,7 +106,18 @@ struct Params {
   unsigned* bound_out;                // [0], [1]: the maxima
   unsigned long long* bound_count;  // entries counted
   int count_only;
+  int64_t unit_begin;  // grouped launches: this problem's first work unit
   unsigned* status;
+};
+
+// A grouped launch of the CTA-pair kernel: many problems, each with its own
+// Params (schedule, sizes, output) and tensor maps, in device memory. Work
+// unit u belongs to the last problem whose unit_begin <= u.
+struct GroupTable {
+  const Params* probs;      // sorted by unit_begin
+  const CUtensorMap* maps;  // [2 * nprobs]: each problem's A map and B half-tile map (64-byte aligned)
+  int nprobs;
+  int64_t units;
 };
 
 __device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0; }
@@ -499,10 +510,10 @@ constexpr int PSTAGES = 7;
 constexpr int P_STAGE_BYTES = A_TILE + B_TILE / 2;  // 32 KB
 constexpr int P_SMEM_BYTES = 1024 + PSTAGES * P_STAGE_BYTES + 256;
 
-template <int KIND, int EPI>
+template <int KIND, int EPI, bool GROUPED = false>
 __global__ void __launch_bounds__(THREADS, 1)
     slice_gemm_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
-                           const __grid_constant__ Params p) {
+                           const __grid_constant__ Params p, const __grid_constant__ GroupTable gt) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + PSTAGES * P_STAGE_BYTES);
@@ -517,22 +528,43 @@ __global__ void __launch_bounds__(THREADS, 1)
   const uint32_t rank = cluster_ctarank();
   const bool leader = (rank == 0);
   const int64_t unit0 = (int64_t)cluster_id_x(), unit_step = (int64_t)cluster_count_x();
-  const int units_m = (p.tiles_m + 1) / 2;
-  const int64_t tile_units = (int64_t)units_m * p.tiles_n;
-  const int gchunk = p.gchunk > 0 ? p.gchunk : p.ngroups;
-  const int64_t units = tile_units * ceil_div_dev(p.ngroups, gchunk);
-  auto g_begin = [&](int64_t t) { return (int)(t / tile_units) * gchunk; };
-  auto g_end = [&](int64_t t) { return min(p.ngroups, g_begin(t) + gchunk); };
+  // A problem's work units: vertical tile pairs x chunks of its groups,
+  // group-major (units in flight read the same digit planes).
+  auto tile_units_of = [](const Params& P) { return (int64_t)((P.tiles_m + 1) / 2) * P.tiles_n; };
+  auto gchunk_of = [](const Params& P) { return P.gchunk > 0 ? P.gchunk : P.ngroups; };
+  const int64_t units = GROUPED ? gt.units : tile_units_of(p) * ceil_div_dev(p.ngroups, gchunk_of(p));
+  unsigned* status = GROUPED ? gt.probs[0].status : p.status;
   // round r hands units [r*step, (r+1)*step) to the CTAs (clusters), in
   // reverse order on odd rounds: units are ordered by falling cost (largest
   // groups first), so this snake order evens out the per-CTA totals
   auto unit_at = [&](int64_t r) {
     return r * unit_step + ((r & 1) ? (unit_step - 1 - unit0) : unit0);
   };
-  auto coords = [&](int64_t t, int& tm, int& tn) {
+  // Calls fn(problem, its A map, its B map, unit within the problem).
+  auto with_unit = [&](int64_t u, auto&& fn) -> bool {
+    if constexpr (GROUPED) {
+      int lo = 0, hi = gt.nprobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (gt.probs[mid].unit_begin <= u) lo = mid;
+        else hi = mid - 1;
+      }
+      const Params& P = gt.probs[lo];
+      return fn(P, &gt.maps[2 * lo], &gt.maps[2 * lo + 1], u - P.unit_begin);
+    } else {
+      return fn(p, &tmA, &tmBh, u);
+    }
+  };
+  // tile of unit t of problem P (rank 1 of an odd last pair reads zero rows, writes nothing)
+  auto coords = [&](const Params& P, int64_t t, int& tm, int& tn) {
     int um;
-    tile_coords<8>(t, units_m, p.tiles_n, um, tn);
-    tm = 2 * um + (int)rank;  // rank 1 of an odd last pair reads zero rows, writes nothing
+    tile_coords<8>(t % tile_units_of(P), (P.tiles_m + 1) / 2, P.tiles_n, um, tn);
+    tm = 2 * um + (int)rank;
+  };
+  auto groups_of = [&](const Params& P, int64_t t, int& g0, int& g1) {
+    const int gc = gchunk_of(P);
+    g0 = (int)(t / tile_units_of(P)) * gc;
+    g1 = min(P.ngroups, g0 + gc);
   };
 
   if (threadIdx.x == 0) {
@@ -561,29 +593,29 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 0) {
     // ------------------------------ TMA producer (both CTAs) ------------------------------
     if (lane == 0) {
-      prefetch_tensormap(&tmA);
-      prefetch_tensormap(&tmBh);
+      if (!GROUPED) {
+        prefetch_tensormap(&tmA);
+        prefetch_tensormap(&tmBh);
+      }
       int stage = 0;
       uint32_t ph = 0;
-      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-        const int64_t t = unit_at(r);
-        if (t >= units) continue;
-        int tm, tn;
-        coords(t % tile_units, tm, tn);
-        for (int g = g_begin(t); g < g_end(t); ++g) {
-          for (int pi = p.group_begin[g]; pi < p.group_begin[g + 1]; ++pi) {
-            for (int kb = 0; kb < p.kblocks; ++kb) {
+      auto produce = [&](const Params& P, const CUtensorMap* mA, const CUtensorMap* mB, int64_t t) -> bool {
+        int tm, tn, g0, g1;
+        coords(P, t, tm, tn);
+        groups_of(P, t, g0, g1);
+        for (int g = g0; g < g1; ++g) {
+          for (int pi = P.group_begin[g]; pi < P.group_begin[g + 1]; ++pi) {
+            for (int kb = 0; kb < P.kblocks; ++kb) {
               if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
-                report_status(p.status, DEV_TIMEOUT_EMPTY);
+                report_status(status, DEV_TIMEOUT_EMPTY);
                 *abort_flag = 1;
-                goto producer_done;
+                return false;
               }
               if (leader) mbar_arrive_expect_tx(&full[stage], 2 * P_STAGE_BYTES);
               uint8_t* sa = smem + stage * P_STAGE_BYTES;
               const uint32_t bar = mapa_shared(&full[stage], 0);
-              tma_load_3d_pair(sa, &tmA, bar, kb * p.kelems, tm * BM, p.pair_a[pi]);
-              tma_load_3d_pair(sa + A_TILE, &tmBh, bar, kb * p.kelems, tn * BN + (int)rank * (BN / 2),
-                               p.pair_b[pi]);
+              tma_load_3d_pair(sa, mA, bar, kb * P.kelems, tm * BM, P.pair_a[pi]);
+              tma_load_3d_pair(sa + A_TILE, mB, bar, kb * P.kelems, tn * BN + (int)rank * (BN / 2), P.pair_b[pi]);
               if (++stage == PSTAGES) {
                 stage = 0;
                 ph ^= 1;
@@ -591,13 +623,20 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
           }
         }
+        return true;
+      };
+      bool ok = true;
+      for (int64_t r = 0; r * unit_step < units && ok && !aborted(abort_flag); ++r) {
+        const int64_t u = unit_at(r);
+        if (u >= units) continue;
+        ok = with_unit(u, produce);
       }
-      if (!aborted(abort_flag)) {
+      if (ok && !aborted(abort_flag)) {
         // every stage released: no commit from the even CTA is still on its
         // way to this CTA's barriers
         for (int i = 0; i < PSTAGES; ++i) {
           if (!mbar_wait_bounded(&empty[stage], ph ^ 1)) {
-            report_status(p.status, DEV_TIMEOUT_EMPTY);
+            report_status(status, DEV_TIMEOUT_EMPTY);
             *abort_flag = 1;
             break;
           }
@@ -607,7 +646,6 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
         }
       }
-    producer_done:;
     }
   } else if (warp == 1) {
     // ------------------------------ MMA issuer (even CTA) ------------------------------
@@ -617,23 +655,23 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0;
       int buf = 0;
       uint32_t acc_ph[2] = {0, 0};
-      for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-        const int64_t t = unit_at(r);
-        if (t >= units) continue;
-        for (int g = g_begin(t); g < g_end(t); ++g) {
+      auto issue = [&](const Params& P, const CUtensorMap*, const CUtensorMap*, int64_t t) -> bool {
+        int g0, g1;
+        groups_of(P, t, g0, g1);
+        for (int g = g0; g < g1; ++g) {
           int load = 0;
           bool open = false;
           uint32_t d_tmem = 0;
-          for (int pp = p.group_begin[g]; pp < p.group_begin[g + 1]; ++pp) {
-            const int w = p.pair_w[pp];
-            if (open && !p.merge_pairs) {
+          for (int pp = P.group_begin[g]; pp < P.group_begin[g + 1]; ++pp) {
+            const int w = P.pair_w[pp];
+            if (open && !P.merge_pairs) {
               tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
               acc_ph[buf] ^= 1;
               buf ^= 1;
               open = false;
             }
-            for (int st = 0; st < p.kblocks;) {
-              if (open && load + w > p.chunk_cap) {
+            for (int st = 0; st < P.kblocks;) {
+              if (open && load + w > P.chunk_cap) {
                 tc::commit2_mc(&tfull[buf], (uint16_t)0x3);
                 acc_ph[buf] ^= 1;
                 buf ^= 1;
@@ -642,9 +680,9 @@ __global__ void __launch_bounds__(THREADS, 1)
               bool fresh = false;
               if (!open) {
                 if (!mbar_wait_bounded(&tempty[buf], acc_ph[buf] ^ 1)) {
-                  report_status(p.status, DEV_TIMEOUT_TMEM);
+                  report_status(status, DEV_TIMEOUT_TMEM);
                   *abort_flag = 1;
-                  goto mma_done;
+                  return false;
                 }
                 tc::fence_after();
                 d_tmem = tmem_base + (uint32_t)(buf * BN);
@@ -652,12 +690,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 open = fresh = true;
               }
               // the k-blocks of this pair that still fit in the open chunk
-              const int s0 = st, s1 = min(p.kblocks, st + (p.chunk_cap - load) / w);
+              const int s0 = st, s1 = min(P.kblocks, st + (P.chunk_cap - load) / w);
               for (; st < s1; ++st) {
                 if (!mbar_wait_bounded(&full[stage], ph)) {
-                  report_status(p.status, DEV_TIMEOUT_FULL);
+                  report_status(status, DEV_TIMEOUT_FULL);
                   *abort_flag = 1;
-                  goto mma_done;
+                  return false;
                 }
                 tc::fence_after();
                 const uint32_t a_addr = smem_u32(smem + stage * P_STAGE_BYTES);
@@ -681,8 +719,14 @@ __global__ void __launch_bounds__(THREADS, 1)
             buf ^= 1;
           }
         }
+        return true;
+      };
+      bool ok = true;
+      for (int64_t r = 0; r * unit_step < units && ok && !aborted(abort_flag); ++r) {
+        const int64_t u = unit_at(r);
+        if (u >= units) continue;
+        ok = with_unit(u, issue);
       }
-    mma_done:
       if (aborted(abort_flag)) {
         tc::commit2_mc(drain, (uint16_t)0x1);
         mbar_wait_bounded(drain, 0);
@@ -696,23 +740,22 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t tempty_leader[2] = {mapa_shared(&tempty[0], 0), mapa_shared(&tempty[1], 0)};
     int buf = 0;
     uint32_t acc_ph[2] = {0, 0};
-    for (int64_t r = 0; r * unit_step < units && !aborted(abort_flag); ++r) {
-      const int64_t t = unit_at(r);
-      if (t >= units) continue;
-      int tm, tn;
-      coords(t % tile_units, tm, tn);
+    auto drain_unit = [&](const Params& P, const CUtensorMap*, const CUtensorMap*, int64_t t) -> bool {
+      int tm, tn, g0, g1;
+      coords(P, t, tm, tn);
+      groups_of(P, t, g0, g1);
       const int64_t row = (int64_t)tm * BM + r_local;
       const int64_t col0 = (int64_t)tn * BN + h * EPI_COLS;
-      if (EPI == EPI_F32) prefetch_c_rows<EPI_COLS>(p, (int64_t)tm * BM + q * 32, col0, lane);
+      if (EPI == EPI_F32) prefetch_c_rows<EPI_COLS>(P, (int64_t)tm * BM + q * 32, col0, lane);
       EpiAcc<EPI> S[EPI_COLS];
 #pragma unroll
       for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
-      for (int g = g_begin(t); g < g_end(t); ++g) {
-        for (int c = 0; c < p.group_chunks[g]; ++c) {
+      for (int g = g0; g < g1; ++g) {
+        for (int c = 0; c < P.group_chunks[g]; ++c) {
           if (!mbar_wait_bounded(&tfull[buf], acc_ph[buf])) {
-            report_status(p.status, DEV_TIMEOUT_MMA);
+            report_status(status, DEV_TIMEOUT_MMA);
             *abort_flag = 1;
-            goto epi_done;
+            return false;
           }
           tc::fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * EPI_COLS);
@@ -724,46 +767,52 @@ __global__ void __launch_bounds__(THREADS, 1)
           buf ^= 1;
         }
         if (EPI == EPI_OZAKI) {
-          if (row < p.m) {
+          if (row < P.m) {
             // tile-blocked plane: this CTA's 128 x 256 tile is one contiguous
             // block, column after column of 128 rows (see the host's plane layout)
-            int* srow = p.sbuf + (size_t)g * p.plane + (size_t)tn * ((size_t)p.tiles_m * BM * BN) +
+            int* srow = P.sbuf + (size_t)g * P.plane + (size_t)tn * ((size_t)P.tiles_m * BM * BN) +
                         (size_t)tm * (BM * BN) + (size_t)(h * EPI_COLS) * BM + r_local;
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) {
               const int64_t col = col0 + j;
-              if (col < p.n) srow[j * BM] = S[j];
+              if (col < P.n) srow[j * BM] = S[j];
             }
           }
 #pragma unroll
           for (int j = 0; j < EPI_COLS; ++j) S[j] = EpiAcc<EPI>(0);
         }
       }
-      if constexpr (EPI == EPI_BOUND) bound_tile<EPI_COLS>(p, row, col0, S);
-      if (EPI == EPI_F32 && row < p.m) {
+      if constexpr (EPI == EPI_BOUND) bound_tile<EPI_COLS>(P, row, col0, S);
+      if (EPI == EPI_F32 && row < P.m) {
         // C is read 8 columns at a time, every load of a group issued before
         // the first use (one memory round trip per group, not per element)
-        float* crow = p.c32 + row * p.rsc;
+        float* crow = P.c32 + row * P.rsc;
 #pragma unroll
         for (int j0 = 0; j0 < EPI_COLS; j0 += 8) {
           float c0[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int64_t col = col0 + j0 + j;
-            c0[j] = (p.beta_f != 0.0f && col < p.n) ? crow[col * p.csc] : 0.0f;
+            c0[j] = (P.beta_f != 0.0f && col < P.n) ? crow[col * P.csc] : 0.0f;
           }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int64_t col = col0 + j0 + j;
-            if (col < p.n) {
-              const float v = (float)S[j0 + j] * p.alpha_f;
-              crow[col * p.csc] = (p.beta_f == 0.0f) ? v : fmaf(p.beta_f, c0[j], v);
+            if (col < P.n) {
+              const float v = (float)S[j0 + j] * P.alpha_f;
+              crow[col * P.csc] = (P.beta_f == 0.0f) ? v : fmaf(P.beta_f, c0[j], v);
             }
           }
         }
       }
+      return true;
+    };
+    bool ok = true;
+    for (int64_t r = 0; r * unit_step < units && ok && !aborted(abort_flag); ++r) {
+      const int64_t u = unit_at(r);
+      if (u >= units) continue;
+      ok = with_unit(u, drain_unit);
     }
-  epi_done:;
   }
 
   __syncwarp();
@@ -819,6 +868,9 @@ inline cudaError_t set_slice_attrs() {
                                        SMEM_BYTES);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(slice_gemm_pair_kernel<KIND, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             P_SMEM_BYTES);
+  if (e == cudaSuccess && EPI == EPI_OZAKI)
+    e = cudaFuncSetAttribute(slice_gemm_pair_kernel<KIND, EPI, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              P_SMEM_BYTES);
   return e;
 }
@@ -925,7 +977,7 @@ inline cudaError_t launch_slice(const CUtensorMap& tmA, const CUtensorMap& tmB_f
     cudaLaunchConfig_t cfg = cluster2_config(P_SMEM_BYTES, attr);
     cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters)));
     cfg.stream = s;
-    return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, q);
+    return cudaLaunchKernelEx(&cfg, slice_gemm_pair_kernel<KIND, EPI>, tmA, tmB_half, q, GroupTable{});
   }
   const int grid = (int)std::min<int64_t>(units, sm_count);
   slice_gemm_kernel<KIND, EPI><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB_full, q);

@@ -143,3 +143,50 @@ def test_autotune_records_and_keeps_c(gpu):
     ref, mag = ou.dd_gemm(A, B, C0)
     assert ou.bound_ratio(tc.cpu().numpy(), ref, mag, k, 2.0**-53) <= 1.0
     gpu.momms_tune_clear()
+
+
+def test_emulated_problems_share_one_slice_launch(gpu):
+    """A plan's emulated problems (uneven sizes, one of a single 128-row tile,
+    different slice counts) run their slice products in one persistent
+    launch, with each result bit-identical to the problem alone; the captured
+    plan relaunches with the same bits."""
+    import torch
+    rng = np.random.default_rng(31)
+    shapes = [(700, 520, 300), (96, 300, 257), (1030, 900, 640), (256, 256, 64), (333, 129, 1000)]
+    slices = [7, 6, 8, 5, 7]
+    descs = (mg.GemmDesc * len(shapes))()
+    keep, host = [], []
+    for i, ((m, n, k), s) in enumerate(zip(shapes, slices)):
+        A = np.asfortranarray(rng.uniform(-1, 1, (m, k)) * np.exp(rng.standard_normal((m, k))))
+        B = np.asfortranarray(rng.uniform(-1, 1, (k, n)))
+        C0 = np.asfortranarray(rng.uniform(-1, 1, (m, n)))
+        ta, ars, acs = gu.to_device(A)
+        tb, brs, bcs = gu.to_device(B)
+        tc, crs, ccs = gu.to_device(C0)
+        descs[i] = gu.make_desc(mg.DTYPE_F64, m, n, k, 1.0 if i % 2 else -0.5, 1.0, (ta.data_ptr(), ars, acs),
+                                (tb.data_ptr(), brs, bcs), (tc.data_ptr(), crs, ccs), precision=mg.PREC_OZAKI,
+                                mem=mg.MEM_DEVICE, slices=s)
+        keep.append((ta, tb, tc))
+        host.append((A, B, C0))
+    expected = [_single(gpu, descs[i], *host[i]) for i in range(len(shapes))]
+    plan = ctypes.c_void_p()
+    mg.check(gpu.momms_plan_create(descs, len(shapes), ctypes.byref(plan)), gpu)
+    gpu.momms_timing_enable(1)
+    gpu.momms_timing_read(mg.KERNEL_SLICE_OZAKI, None, None, 1)
+    mg.check(gpu.momms_plan_launch(plan, None), gpu)
+    torch.cuda.synchronize()
+    launches = ctypes.c_ulonglong(0)
+    gpu.momms_timing_read(mg.KERNEL_SLICE_OZAKI, None, ctypes.byref(launches), 1)
+    gpu.momms_timing_enable(0)
+    assert launches.value == 1  # one slice launch for all five problems
+    for i in range(len(shapes)):
+        assert np.array_equal(keep[i][2].cpu().numpy(), expected[i]), i
+    mg.check(gpu.momms_plan_capture(plan, None), gpu)
+    for rep in range(2):
+        for i in range(len(shapes)):
+            keep[i][2].copy_(torch.from_numpy(np.ascontiguousarray(host[i][2].T)).t())
+        mg.check(gpu.momms_plan_launch(plan, None), gpu)
+        torch.cuda.synchronize()
+        for i in range(len(shapes)):
+            assert np.array_equal(keep[i][2].cpu().numpy(), expected[i]), (rep, i)
+    mg.check(gpu.momms_plan_destroy(plan), gpu)
