@@ -361,32 +361,96 @@ def _time_on(torch, stream, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
+def _tune_summary(lib, mg):
+    """The tuning table's choices, counted per dtype: tiles and split counts."""
+    need = ctypes.c_size_t(0)
+    mg.check(lib.momms_tune_export(None, 0, ctypes.byref(need)), lib)
+    buf = ctypes.create_string_buffer(max(1, need.value))
+    mg.check(lib.momms_tune_export(buf, need.value, None), lib)
+    out = {}
+    for line in buf.value.decode().split("\n"):
+        f = line.split()
+        if len(f) < 6:
+            continue
+        dt = "f64" if f[0] == "0" else "f32"
+        tile = "128x128" if (len(f) < 7 or f[6] == "0") else "64x64"
+        e = out.setdefault(dt, {"buckets": 0, "tiles": {}, "splits": {}})
+        e["buckets"] += 1
+        e["tiles"][tile] = e["tiles"].get(tile, 0) + 1
+        e["splits"][f[5]] = e["splits"].get(f[5], 0) + 1
+    return out
+
+
 def measure_batched(lib, mg, torch, dev):
     """512 uneven problems (m, n, k log-uniform over [32, 1024], half f64 and
     half f32, plain) as one plan launched through its CUDA graph, against one
-    momms_gemm launch per problem."""
+    momms_gemm launch per problem; per-kernel rates of the grouped DMMA and
+    FFMA launches against their measured peaks, with the configuration model
+    and with the table momms_autotune_batch fills."""
     count = 512
     descs, keep, flops = _problem_set(mg, torch, dev, count, 32, 1024, 512, [0.5, 0.0, 0.5])
+    f64_flops = sum(2.0 * d.m * d.n * d.k for d in descs if d.dtype == mg.DTYPE_F64)
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
-    plan = ctypes.c_void_p()
-    mg.check(lib.momms_plan_create(descs, count, ctypes.byref(plan)), lib)
-    mg.check(lib.momms_plan_capture(plan, sp), lib)
-    t_graph = _time_on(torch, stream, lambda: mg.check(lib.momms_plan_launch(plan, sp), lib), 5)
+    pk = {}
+    for kind, name in ((0, "fp64_dmma"), (1, "ffma")):
+        v = ctypes.c_double(0.0)
+        mg.check(lib.momms_measure_peak(kind, ctypes.byref(v)), lib)
+        pk[name] = v.value
+
+    def run_plan():
+        plan = ctypes.c_void_p()
+        mg.check(lib.momms_plan_create(descs, count, ctypes.byref(plan)), lib)
+        # per-kernel device time from uncaptured launches (events per launch)
+        lib.momms_timing_enable(1)
+        for kc in (mg.KERNEL_DGEMM_DMMA, mg.KERNEL_SGEMM_FFMA):
+            lib.momms_timing_read(kc, None, None, 1)
+        reps = 3
+        for _ in range(reps):
+            mg.check(lib.momms_plan_launch(plan, sp), lib)
+        stream.synchronize()
+        ms = {}
+        for kc, name in ((mg.KERNEL_DGEMM_DMMA, "f64"), (mg.KERNEL_SGEMM_FFMA, "f32")):
+            t = ctypes.c_double(0)
+            lib.momms_timing_read(kc, ctypes.byref(t), None, 1)
+            ms[name] = t.value / reps
+        lib.momms_timing_enable(0)
+        mg.check(lib.momms_plan_capture(plan, sp), lib)
+        t_graph = _time_on(torch, stream, lambda: mg.check(lib.momms_plan_launch(plan, sp), lib), 5)
+        lib.momms_plan_destroy(plan)
+        f64_tf = f64_flops / (ms["f64"] * 1e-3) / 1e12 if ms["f64"] else None
+        f32_tf = (flops - f64_flops) / (ms["f32"] * 1e-3) / 1e12 if ms["f32"] else None
+        return {"grouped_graph_ms": t_graph, "grouped_tflops": flops / (t_graph * 1e-3) / 1e12,
+                "f64_kernel_ms": ms["f64"], "f64_tflops": f64_tf,
+                "f64_frac_of_dmma_peak": f64_tf / pk["fp64_dmma"] if f64_tf else None,
+                "f32_kernel_ms": ms["f32"], "f32_tflops": f32_tf,
+                "f32_frac_of_ffma_peak": f32_tf / pk["ffma"] if f32_tf else None}
+
+    lib.momms_tune_clear()
+    model = run_plan()
 
     def singles():
         for i in range(count):
             mg.check(lib.momms_gemm(ctypes.byref(descs[i]), sp), lib)
     t_single = _time_on(torch, stream, singles, 2)
-    lib.momms_plan_destroy(plan)
+    tuned_n = ctypes.c_int32(0)
+    t0 = time.perf_counter()
+    mg.check(lib.momms_autotune_batch(descs, count, sp, ctypes.byref(tuned_n)), lib)
+    tune_s = time.perf_counter() - t0
+    tuned = run_plan()
+    tuned["buckets_tuned"] = tuned_n.value
+    tuned["tuning_s"] = tune_s
+    tuned["choices"] = _tune_summary(lib, mg)
+    lib.momms_tune_clear()
     del keep
     return {"workload": "512 problems, m,n,k log-uniform [32,1024] (seed 512), half f64 half f32, plain",
-            "grouped_graph_ms": t_graph, "per_problem_launches_ms": t_single,
-            "grouped_tflops": flops / (t_graph * 1e-3) / 1e12, "speedup_vs_per_problem": t_single / t_graph,
-            "launches_per_batch": "one graph launch (one persistent kernel per dtype)"}
+            "peaks_tflops": pk, "model": model, "tuned": tuned,
+            "grouped_graph_ms": model["grouped_graph_ms"], "per_problem_launches_ms": t_single,
+            "grouped_tflops": model["grouped_tflops"], "speedup_vs_per_problem": t_single / model["grouped_graph_ms"],
+            "launches_per_batch": "one graph launch (one persistent kernel per dtype and tile)"}
 
 
-def measure_serving(lib, mg, torch, dev, rates=(400.0, 1600.0, 3200.0), count=2000):
+def measure_serving(lib, mg, torch, dev, rates=(400.0, 1000.0, 1200.0, 1600.0), count=2000):
     """Poisson arrivals of mixed requests (m, n, k log-uniform over [64, 4096];
     40% f64 plain, 40% f64 emulated at a 1e-14 target, 20% f32) with operands
     resident in HBM under a 60 GiB budget; latency percentiles and throughput
@@ -569,14 +633,14 @@ def run_ours(args):
     dmma_ms, dmma_n = _kernel_ms(lib, mg, mg.KERNEL_DGEMM_DMMA)
     C_plain = dC.t().cpu().numpy().T
     err_plain = sampled_error(A, B, C0, C_plain)
-    for cls in range(6):
+    for cls in range(mg.KERNEL_CLASSES):
         _kernel_ms(lib, mg, cls)  # reset
 
     # ---- emulated FP64: the timed region of the headline value ----
     clocks = ClockSampler(local)
     clocks.start()
     _timed_steps(lib, mg, torch, stream, emu_desc, dC, dC0, 0, args.warmup)
-    for cls in range(6):
+    for cls in range(mg.KERNEL_CLASSES):
         _kernel_ms(lib, mg, cls)  # reset: count the timed steps only
     barrier(world)
     torch.cuda.synchronize()
@@ -591,6 +655,7 @@ def run_ours(args):
     slice_ms, slice_n = _kernel_ms(lib, mg, mg.KERNEL_SLICE_OZAKI)
     prep_ms, _ = _kernel_ms(lib, mg, mg.KERNEL_PREP)
     comb_ms, _ = _kernel_ms(lib, mg, mg.KERNEL_COMBINE)
+    bound_ms, _ = _kernel_ms(lib, mg, mg.KERNEL_BOUND)
     lib.momms_timing_enable(0)
     total_ms = max_over_ranks(sum(step_ms), world)
     ms_per_step = total_ms / args.steps
@@ -678,7 +743,8 @@ def run_ours(args):
                                 0: "momms::sp::slice_gemm_kernel<kind::f16, Ozaki>"}.get(info.slice_variant, "?"),
                      "algorithmic_flops_per_launch": tc_flops_per_launch,
                      "kernel_ms_per_launch": slice_avg, "launches_per_step": slice_per_step,
-                     "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps}},
+                     "other_kernels_ms_per_step": {"prep": prep_ms / args.steps, "combine": comb_ms / args.steps,
+                                                   "bound": bound_ms / args.steps}},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "api": "momms_gemm, MOMMS_PREC_OZAKI, MOMMS_MEM_HOST pinned operands"},
         "gpu_launches": int(launches),

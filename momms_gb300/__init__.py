@@ -33,6 +33,7 @@ KERNEL_SLICE_TF32 = 3
 KERNEL_PREP = 4
 KERNEL_COMBINE = 5
 KERNEL_BOUND = 6
+KERNEL_CLASSES = 7
 
 FAULT_ALLOC = 0
 FAULT_CUDA = 1

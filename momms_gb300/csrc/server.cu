@@ -15,7 +15,12 @@
 // batch's completion event. Each batch also carries two timing events on its
 // stream, around its launch: their times relative to an event recorded when
 // the server starts are the batch's device interval, reported per request, so
-// that the overlap of batches on the GPU can be read off directly.
+// that the overlap of batches on the GPU can be read off directly. NVTX
+// ranges mark each batch's formation and launch on the scheduler thread and
+// each completion (header-only NVTX v3: no cost unless a profiler attaches).
+#include <nvtx3/nvToolsExt.h>
+#include <stdio.h>
+
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -147,6 +152,11 @@ struct Server {
           cudaGetLastError();
           t_start = t_end = -1.0f;
         }
+        {
+          char msg[96];
+          snprintf(msg, sizeof(msg), "momms batch %llu done (%zu requests)", (unsigned long long)b.id, b.ids.size());
+          nvtxMarkA(msg);
+        }
         for (uint64_t id : b.ids) {
           Request& r = reqs[id];
           r.batch_id = b.id;
@@ -218,6 +228,12 @@ struct Server {
         launching += 1;  // in no queue while the lock is released
         lk.unlock();
         cudaStream_t s = streams[sidx];
+        {
+          char msg[96];
+          snprintf(msg, sizeof(msg), "momms batch %llu: plan + launch (%zu requests, stream %d)",
+                   (unsigned long long)next_batch, descs.size(), sidx);
+          nvtxRangePushA(msg);
+        }
         int rc = plan_create(descs.data(), (int)descs.size(), &b.plan, s, true);
         cudaError_t e = cudaSuccess;
         if (!rc) {
@@ -232,6 +248,7 @@ struct Server {
         // only when that work is: its requests' outputs are not touched again
         // once they are reported.
         if (rc) cudaStreamSynchronize(s);
+        nvtxRangePop();
         lk.lock();
         launching -= 1;
         if (rc) {

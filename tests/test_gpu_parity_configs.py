@@ -160,3 +160,19 @@ def test_ffma_offsets_beyond_32_bits(gpu):
     torch.cuda.empty_cache()
     ref, mag = ou.dd_gemm(np.asfortranarray(A), B, C0)
     assert ou.bound_ratio(C, ref, mag, k, U32) <= 1.0
+
+
+def test_slice_sweep_script_small(gpu):
+    """tests/slice_sweep.py at 512^3, phi = 2: every entry checked; the error
+    never grows with a slice added, and the automatic count's stated bound
+    holds."""
+    from tests import slice_sweep
+    rows = slice_sweep.sweep([512], phis=(2.0,), slice_range=range(3, 7), out=open("/dev/null", "w"))
+    fixed = [r for r in rows if r["slices"].isdigit()]
+    assert [r["used"] for r in fixed] == [3, 4, 5, 6]
+    errs = [r["err"] for r in fixed]
+    assert all(b <= a for a, b in zip(errs, errs[1:])), errs
+    auto = rows[-1]
+    assert auto["slices"].startswith("auto") and auto["err"] <= auto["bound"] + 4 * U64
+    assert all(r["entries_checked"] == 512 * 512 for r in rows)
+    assert "| 512 | 2.0 | auto 1e-14 |" in slice_sweep.table(rows)

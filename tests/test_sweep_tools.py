@@ -48,3 +48,14 @@ def test_roofline_bound():
     assert abs(o["bound_tflops"] - flops / bytes_ * 6760.6 / 1e3) < 1e-9 and o["bound_tflops"] < 78.0
     assert "bound_tflops" not in sweep.roofline({"dtype": "f64", "prec": "ozaki", "m": 64, "n": 64, "k": 64,
                                                  "ms": 1.0, "tflops": 1.0}, pk)
+
+
+def test_slice_sweep_table_format():
+    from tests import slice_sweep
+    rows = [{"s": 2048, "phi": 0.5, "slices": "plain", "used": 0, "ms": 18.7, "tflops": 0.92, "err": 1.1e-16,
+             "bound": None, "unreachable": False, "entries_checked": 2048 * 2048},
+            {"s": 2048, "phi": 8.0, "slices": "auto 1e-14", "used": 15, "ms": 2.0, "tflops": 8.6, "err": 3e-15,
+             "bound": 2e-12, "unreachable": True, "entries_checked": 2048 * 2048}]
+    t = slice_sweep.table(rows).split("\n")
+    assert len(t) == 4 and t[2].startswith("| 2048 | 0.5 | plain | — |")
+    assert "(target unreachable)" in t[3]
