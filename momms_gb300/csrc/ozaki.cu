@@ -841,6 +841,19 @@ __device__ __forceinline__ void magnitude(double v, int e, bool indicator, uint1
     return;
   }
   const int be = (int)(ab >> 52);
+  if (be != 0 && be - 1023 - e <= -1) {
+    // normal v below 2^e (every element of a row but subnormals):
+    // |v| 2^-e in [2^X, 2^(X+1)) with X = be - 1023 - e. The bf16's 7
+    // fraction bits are the top of v's fraction, and |v| 2^(40-e) =
+    // M 2^-(12-X) is a right shift by at least 13: the general steps below,
+    // with the shift counts known.
+    const int X = be - 1023 - e;
+    if (X + 127 >= 1) *bf = (uint16_t)(((unsigned)(X + 127) << 7) | ((unsigned)(ab >> 45) & 0x7fu));
+    const int r = 12 - X;
+    const unsigned long long M = (ab & ((1ull << 52) - 1)) | (1ull << 52);
+    *fix = r < 64 ? (M >> r) + ((M << (64 - r)) != 0 ? 1ull : 0ull) : 1ull;
+    return;
+  }
   const unsigned long long M = be ? ((ab & ((1ull << 52) - 1)) | (1ull << 52)) : ab;
   const int E = be ? be - 1075 : -1074;           // |v| = M 2^E
   const int nb = 64 - __clzll((long long)M);      // significant bits of M
