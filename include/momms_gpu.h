@@ -303,7 +303,8 @@ int momms_tune_export(char* buf, size_t cap, size_t* needed);
 int momms_tune_import(const char* text);
 int momms_tune_clear(void);
 
-/* What the calling thread's last successful momms_gemm did. No reference
+/* What the calling thread's last momms_gemm that wrote C did (MOMMS_OK, or
+ * MOMMS_ERR_TARGET_UNREACHABLE with the 15-slice result). No reference
  * counterpart (the reference's blocking is fixed at compile time). */
 typedef struct {
   int32_t precision;      /* momms_precision actually run */
