@@ -154,6 +154,13 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// signed 32 x 32 -> 64-bit product plus c, one instruction
+__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
+  long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+
 __device__ __forceinline__ void report_status(unsigned* status, unsigned bit) {
   if (status) atomicOr(status, bit);
 }

@@ -375,13 +375,6 @@ struct CombineParams {
   int64_t rsc, csc;
 };
 
-// signed 32 x 32 -> 64-bit product plus c, one instruction
-__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
-  long long d;
-  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-  return d;
-}
-
 // Thread rows i and i + 256 of block row blockIdx.x, for columns
 // j0 + blockIdx.y, stepping by gridDim.y: no index division, the row
 // exponents stay in registers, and the two rows' loads are in flight together.
