@@ -87,17 +87,27 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restric
       if (mx) atomicMax(&maxbits[r], mx);
     }
   } else {
-    // one warp per row, lanes along p
+    // one warp per row, lanes along p; all 32 loads of a thread in flight
+    // before the first maximum
+    double v[4][8];
+#pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int64_t r = r0 + ty + 8 * i;
-      if (r >= R) break;
-      unsigned long long mx = 0;
+#pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int64_t pp = p0 + tx + 32 * j;
-        if (pp < K) mx = max(mx, abs_bits(x[r * sr + pp * sp]));
+        v[i][j] = (r < R && pp < K) ? x[r * sr + pp * sp] : 0.0;
       }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t r = r0 + ty + 8 * i;
+      unsigned long long mx = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) mx = max(mx, abs_bits(v[i][j]));
+#pragma unroll
       for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (tx == 0 && mx) atomicMax(&maxbits[r], mx);
+      if (tx == 0 && mx && r < R) atomicMax(&maxbits[r], mx);
     }
   }
 }
@@ -868,38 +878,33 @@ __device__ __forceinline__ void magnitude(double v, int e, bool indicator, uint1
 // warp and posts one 64-bit atomicAdd (exact, so the sums do not depend on
 // timing). With `indicator` it writes the 0/1 plane of nonzero elements and
 // no sums.
+template <bool R_CONTIG>
 __global__ void __launch_bounds__(256) magnitude_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
-                                                        int64_t R, int64_t K, bool r_contig,
-                                                        const int* __restrict__ exps, uint16_t* __restrict__ plane,
-                                                        int64_t ldp, unsigned long long* __restrict__ sums,
-                                                        bool indicator) {
-  constexpr int TR = 32, TP = 64;
+                                                        int64_t R, int64_t K, const int* __restrict__ exps,
+                                                        uint16_t* __restrict__ plane, int64_t ldp,
+                                                        unsigned long long* __restrict__ sums, bool indicator) {
+  constexpr int TR = planes::TILE_R, TP = planes::TILE_P;
+  static_assert(planes::THREADS == 256, "one warp per 8th row of the tile");
   __shared__ double tile[TR][TP + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t p0 = (int64_t)blockIdx.x * TP;
+  const int64_t pp = p0 + 2 * lane;
   for (int64_t r0 = (int64_t)blockIdx.y * TR; r0 < R; r0 += (int64_t)gridDim.y * TR) {
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < TR * TP / 256; ++i) {
-      const int lin = tid + 256 * i;
-      const int rl = r_contig ? (lin % TR) : (lin / TP);
-      const int pl = r_contig ? (lin / TR) : (lin % TP);
-      const int64_t r = r0 + rl, pp = p0 + pl;
-      tile[rl][pl] = (r < R && pp < K) ? x[r * sr + pp * sp] : 0.0;
-    }
+    planes::stage_tile<R_CONTIG>(x, sr, sp, R, K, r0, p0, tile);
     __syncthreads();
+    uint16_t* out = plane + (r0 + warp) * ldp + pp;
 #pragma unroll 1
-    for (int rl = warp; rl < TR; rl += 8) {
+    for (int rl = warp; rl < TR; rl += 8, out += 8 * ldp) {
       const int64_t r = r0 + rl;
       if (r >= R) break;  // uniform over the warp
       const int e = exps[r];
-      const int64_t pp = p0 + 2 * lane;
       uint16_t b0 = 0, b1 = 0;
       unsigned long long f0 = 0, f1 = 0;
       if (pp < K) {
         magnitude(tile[rl][2 * lane], e, indicator, &b0, &f0);
         magnitude(tile[rl][2 * lane + 1], e, indicator, &b1, &f1);  // beyond K: the tile holds 0
-        *reinterpret_cast<unsigned*>(plane + r * ldp + pp) = (unsigned)b0 | ((unsigned)b1 << 16);
+        *reinterpret_cast<unsigned*>(out) = (unsigned)b0 | ((unsigned)b1 << 16);
       }
       if (!indicator) {
         unsigned long long t = f0 + f1;
@@ -918,7 +923,8 @@ int enqueue_magnitudes(const double* x, int64_t sr, int64_t sp, int64_t R, int64
   dim3 grid((unsigned)ceil_div(K, 64), (unsigned)std::min<int64_t>(ceil_div(R, 32), 65535));
   {
     KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    magnitude_kernel<<<grid, 256, 0, s>>>(x, sr, sp, R, K, r_contig, exps, plane, kp, sums, indicator);
+    if (r_contig) magnitude_kernel<true><<<grid, 256, 0, s>>>(x, sr, sp, R, K, exps, plane, kp, sums, indicator);
+    else magnitude_kernel<false><<<grid, 256, 0, s>>>(x, sr, sp, R, K, exps, plane, kp, sums, indicator);
   }
   note_launch();
   const cudaError_t e = launch_status();
