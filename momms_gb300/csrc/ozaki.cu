@@ -994,11 +994,12 @@ int enqueue_bound_kernel(const BoundWork& w, int64_t m, int64_t n, int64_t k, bo
 
 // The bound's result, once the bound kernel is enqueued on `s`: the two
 // maxima, and whether some entry is uncovered. The kernel counts the entries
-// with a positive lower bound; if that is not all of C, a second pass over
-// 0/1 indicator planes counts the entries with any nonzero product term. An
-// entry counted there but not by the bound has every term below FP32's range
-// (relative to 2^(e_i+f_j)): no slice count can vouch for it. Entries with no
-// nonzero term are exact (their digits are all zero). Synchronises `s`.
+// whose lower bound is zero (none, for dense data); if there are any, a
+// second pass over 0/1 indicator planes counts the entries with any nonzero
+// product term. An entry counted there but without a positive bound has every
+// term below FP32's range (relative to 2^(e_i+f_j)): no slice count can vouch
+// for it. Entries with no nonzero term are exact (their digits are all zero).
+// Synchronises `s`.
 struct OperandViews {
   const double* a;
   int64_t a_rs, a_cs;
@@ -1015,10 +1016,11 @@ int bound_result(const BoundWork& w, const OperandViews& v, int64_t m, int64_t n
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound");
   memcpy(q1, &words[0], 4);
   memcpy(q2, &words[1], 4);
-  unsigned long long covered;
-  memcpy(&covered, &words[2], 8);
+  unsigned long long zeros;
+  memcpy(&zeros, &words[2], 8);
   *uncovered = false;
-  if (covered >= (unsigned long long)m * (unsigned long long)n) return MOMMS_OK;
+  if (zeros == 0) return MOMMS_OK;
+  const unsigned long long covered = (unsigned long long)m * (unsigned long long)n - zeros;
   // indicator pass (sparse operands, or terms beyond FP32's range)
   ce = cudaMemsetAsync(w.out + 2, 0, 8, s);
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki bound");

@@ -33,7 +33,7 @@
 //                 q1 = (sum_p |a_ip| 2^-e_i + sum_p |b_pj| 2^-f_j) / L_ij,
 //                 q2 = k / L_ij
 //               (upward-rounded) to two maxima posted with atomicMax, and
-//               counts the entries with L_ij > 0, from which the host picks a
+//               counts the entries with L_ij = 0; from these the host picks a
 //               slice count that holds for every entry. With count_only the
 //               planes are 0/1 indicators of nonzero elements and only the
 //               entries with a nonzero sum are counted.
@@ -174,21 +174,29 @@ __device__ __forceinline__ void bound_tile(const Params& p, int64_t row, int64_t
     for (int j = 0; j < NC; ++j) cnt += (col0 + j < p.n && S[j] > 0.0f) ? 1u : 0u;
   } else if (row < p.m) {
     const float sa = __fmul_ru(__ull2float_ru(p.msum_a[row]), 0x1p-40f);
-    float r2 = 0.0f;  // largest 1 / L over the row (q2 = k / L)
+    // q2 = k / L needs only the row's smallest L: one reciprocal per row.
+    // q1 = (sa + sb) / L: an entry whose (sa + sb), rounded up, is at most
+    // m1 * L rounded down cannot raise m1 (its quotient is at most m1), so
+    // the upward quotient is formed only for the others.
+    float lmin = INFINITY;
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
       const int64_t col = col0 + j;
       const float lb = __fmul_rd(S[j], p.lb_scale);
-      // L = 0: no p with both a_ip and b_pj nonzero, so the entry has no error
-      if (col < p.n && lb > 0.0f) {
-        const float r = __frcp_ru(lb);  // >= 1 / L
-        const float sb = __fmul_ru(__ull2float_ru(p.msum_b[col]), 0x1p-40f);
-        m1 = fmaxf(m1, __fmul_ru(__fadd_ru(sa, sb), r));
-        r2 = fmaxf(r2, r);
-        ++cnt;
+      // L = 0: no p with both a_ip and b_pj nonzero (the entry has no
+      // error), or every term below FP32's range: counted, the host tells
+      // the two apart
+      if (col < p.n) {
+        if (lb > 0.0f) {
+          const float x = __fadd_ru(sa, __fmul_ru(__ull2float_ru(p.msum_b[col]), 0x1p-40f));
+          if (x > __fmul_rd(m1, lb)) m1 = fmaxf(m1, __fmul_ru(x, __frcp_ru(lb)));
+          lmin = fminf(lmin, lb);
+        } else {
+          ++cnt;
+        }
       }
     }
-    m2 = __fmul_ru(p.kf, r2);
+    if (lmin < INFINITY) m2 = __fmul_ru(p.kf, __frcp_ru(lmin));  // >= k / L for every entry of the row
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -197,10 +205,14 @@ __device__ __forceinline__ void bound_tile(const Params& p, int64_t row, int64_t
     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    // non-negative floats order like their bit patterns
+    // Non-negative floats order like their bit patterns. Every warp of every
+    // tile reports here: the maxima only grow, so a warp below the value
+    // already posted skips its atomic (same-address atomics serialise in L2;
+    // at 8192 x 8192 x 64 they cost most of the kernel).
     if (!p.count_only) {
-      atomicMax(&p.bound_out[0], __float_as_uint(m1));
-      atomicMax(&p.bound_out[1], __float_as_uint(m2));
+      const volatile unsigned* cur = p.bound_out;
+      if (__float_as_uint(m1) > cur[0]) atomicMax(&p.bound_out[0], __float_as_uint(m1));
+      if (__float_as_uint(m2) > cur[1]) atomicMax(&p.bound_out[1], __float_as_uint(m2));
     }
     if (cnt) atomicAdd(p.bound_count, (unsigned long long)cnt);
   }

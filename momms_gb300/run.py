@@ -79,7 +79,7 @@ def main():
         torch.cuda.synchronize()
         names = {mg.KERNEL_DGEMM_DMMA: "dgemm_dmma", mg.KERNEL_SGEMM_FFMA: "sgemm_ffma",
                  mg.KERNEL_SLICE_OZAKI: "slice_ozaki", mg.KERNEL_SLICE_TF32: "slice_tf32",
-                 mg.KERNEL_PREP: "prep", mg.KERNEL_COMBINE: "combine"}
+                 mg.KERNEL_PREP: "prep", mg.KERNEL_COMBINE: "combine", mg.KERNEL_BOUND: "bound"}
         per = {}
         for cls, name in names.items():
             tot, cnt = ctypes.c_double(), ctypes.c_ulonglong()
