@@ -13,19 +13,21 @@
 // kind::f16 with FP32 accumulation in TMEM, and every accumulation chunk's
 // sum of absolute products is kept at or below 2^24, so that every partial
 // sum is an exactly representable integer; chunks are gathered in int32
-// registers, and the diagonals are combined exactly in 128-bit integers
-// (Horner's rule over the diagonals) and rounded once to FP64. See
-// slicegemm.cuh for the engine. With 8-bit digits 7 slices cover 56 bits with
+// registers, and the diagonals are combined exactly (64-bit partial sums per
+// 32-bit word offset, up to 148 bits) and rounded once to FP64
+// (exact_round.cuh). See slicegemm.cuh for the engine. With 8-bit digits 7 slices cover 56 bits with
 // 28 slice products, where 7-bit digits need 8 slices and 36 products; the
 // price is 4x larger products, so TMEM is drained every 4 (top x top), 8 (top
 // x centred) or 16 (centred x centred) k-blocks.
 //
 // The slice count is chosen per call from the requested componentwise error
-// (|dC_ij| / (|A||B|)_ij) with a bound evaluated on sampled entries: with RN
-// digits the truncation error is at most
+// (|dC_ij| / (|A||B|)_ij): with RN digits the truncation error is at most
 //   2^(-bits*s-1) * (2^e_i sum_p |b_pj| + 2^f_j sum_p |a_ip|
 //                    + (s-1)/2 * k * 2^(e_i+f_j))
-// (digit truncation of A and B, then the largest dropped diagonal).
+// (digit truncation of A and B, then the largest dropped diagonal), and the
+// bound kernel bounds (|A||B|)_ij from below for every entry, so the count
+// holds for every entry of C (a sampled estimate starts host-staged calls
+// early; the bound then verifies it before C is written).
 #include <cuda_fp16.h>
 #include <math.h>
 #include <stdlib.h>
@@ -357,14 +359,15 @@ __global__ void __launch_bounds__(32) sample_final_kernel(const double* __restri
 // with R rounded to double once. All the summation is integer arithmetic;
 // FP64 is used for the final conversion, scaling and beta update only.
 //
-// R is formed from four 64-bit partial sums, one per 32-bit word offset:
-// group g's weight 2^sh (sh = bits*(dmax - level) <= 112) is split into a
-// word gw[g] = sh / 32 and a shift gb[g] = sh % 32 <= 24, so that
-// R = P0 + P1 2^32 + P2 2^64 + P3 2^96 with P_w = sum over the groups of word
-// w of S_g 2^gb[g]: each term is below 2^55 and a word holds at most four
-// levels (at most eight groups each), so no partial sum leaves 64 bits. Every
-// level enters exactly, up to the most slices (dmax = 14), and R is rounded
-// once (wide_to_double).
+// R is formed from 64-bit partial sums, one per 32-bit word offset (four at
+// 13-15 slices, three below): group g's weight 2^sh (sh = bits*(dmax -
+// level) <= 112) is split into a word gw[g] = sh / 32 and a shift
+// gb[g] = sh % 32 <= 24, so that R = P0 + P1 2^32 + P2 2^64 + P3 2^96 with
+// P_w = sum over the groups of word w of S_g 2^gb[g]: each term is below 2^55
+// and a word holds at most four levels (at most eight groups each), so no
+// partial sum leaves 64 bits. Every level enters exactly, up to the most
+// slices (dmax = 14), and R is rounded once (i128_to_double / wide_to_double,
+// exact_round.cuh).
 struct CombineParams {
   const int* sbuf;  // tile-blocked group planes (sp::Params::sbuf)
   int64_t plane;

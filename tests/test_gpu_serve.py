@@ -130,3 +130,42 @@ def test_budget_holds_back_but_completes(gpu):
     for rid in ids:
         assert gpu.momms_server_poll(srv, rid, None) == mg.OK
     mg.check(gpu.momms_server_destroy(srv), gpu)
+
+
+def test_emulated_requests_of_a_batch_share_one_slice_launch(gpu):
+    """Emulated requests submitted together land in one batch, whose plan runs
+    their slice products in one persistent launch; each result still equals
+    the request run alone."""
+    import torch
+    rng = np.random.default_rng(71)
+    reqs = [_request(rng, "ozaki", lo=200, hi=600) for _ in range(6)]
+    expected = [_alone(gpu, d, *host) for d, _, host in reqs]
+    cfg = mg.ServerConfig(hbm_budget_bytes=8 << 30, max_batch=16, max_inflight=1, queue_capacity=64)
+    srv = ctypes.c_void_p()
+    gpu.momms_timing_enable(1)
+    gpu.momms_timing_read(mg.KERNEL_SLICE_OZAKI, None, None, 1)
+    gpu.momms_timing_read(mg.KERNEL_BOUND, None, None, 1)
+    # the server starts with the queue already full: one batch takes all six
+    mg.check(gpu.momms_server_create(ctypes.byref(cfg), ctypes.byref(srv)), gpu)
+    ids = []
+    for d, _, _ in reqs:
+        rid = ctypes.c_uint64(0)
+        mg.check(gpu.momms_server_submit(srv, ctypes.byref(d), ctypes.byref(rid)), gpu)
+        ids.append(rid.value)
+    mg.check(gpu.momms_server_drain(srv, 60.0), gpu)
+    batches = set()
+    for rid in ids:
+        info = mg.RequestInfo()
+        mg.check(gpu.momms_server_poll(srv, rid, ctypes.byref(info)), gpu)
+        assert info.status == mg.OK
+        batches.add(info.batch_id)
+    mg.check(gpu.momms_server_destroy(srv), gpu)
+    torch.cuda.synchronize()
+    slice_launches = ctypes.c_ulonglong(0)
+    gpu.momms_timing_read(mg.KERNEL_SLICE_OZAKI, None, ctypes.byref(slice_launches), 1)
+    gpu.momms_timing_enable(0)
+    # one slice launch per batch (the slice-count choice at plan creation
+    # runs the bound kernel per problem, counted in its own class)
+    assert slice_launches.value == len(batches) < len(reqs)
+    for (d, dev, host), exp in zip(reqs, expected):
+        assert np.array_equal(dev[2].cpu().numpy(), exp)
