@@ -172,34 +172,37 @@ struct OzakiSliceOp {
   using Tout = __half;
   using U = typename std::conditional<(kDigitBits * NS <= 62), unsigned long long, unsigned __int128>::type;
   const int* exps;
+  // 32-bit word w of Y
+  __device__ __forceinline__ static uint32_t word(U y, int w) { return (uint32_t)(y >> (32 * w)); }
   __device__ __forceinline__ void pair(double v0, double v1, int64_t r, __half* out, int64_t plane_elems) const {
-    constexpr int bits = kDigitBits, half = 1 << (bits - 1);
-    constexpr unsigned mask = (1u << bits) - 1u;
+    constexpr int bits = kDigitBits;
+    static_assert(bits == 8, "lower digits are the bytes of Y");
     const int e = exps[r];
     const U Y0 = offset_digits<NS, U>(v0, e), Y1 = offset_digits<NS, U>(v1, e);
     const bool n0 = __double_as_longlong(v0) < 0, n1 = __double_as_longlong(v1) < 0;
     static_assert(2 * (1 << bits) < 1024, "digits must fit the 0x6400 pattern");
     constexpr unsigned short kBias = 0x6400 + (1u << bits);  // 1024 + 2^bits
     const __half2 bias = __halves2half2(__ushort_as_half(kBias), __ushort_as_half(kBias));
+    // A lower digit d = byte - 2^(bits-1) of a value of sign n is held as
+    // u = (n ? -d : d) + 2^bits, that is byte + 128 or (byte ^ 0xff) + 129:
+    // for both elements of the pair at once, bytes in 16-bit lanes 0 and 1.
+    const uint32_t flip = (n0 ? 0xffu : 0u) | (n1 ? 0xff0000u : 0u);
+    const uint32_t add = 0x64006400u + ((n0 ? 129u : 128u) | ((n1 ? 129u : 128u) << 16));
     // least significant position first, into the last plane, walking back
-    U y0 = Y0, y1 = Y1;
     __half* o = out + (int64_t)(NS - 1) * plane_elems;
 #pragma unroll
-    for (int pos = 0; pos < NS; ++pos) {
-      int d0, d1;
-      if (pos == NS - 1) {  // top digit: the remaining bits
-        d0 = (int)(unsigned)y0;
-        d1 = (int)(unsigned)y1;
-      } else {
-        d0 = (int)((unsigned)y0 & mask) - half;
-        d1 = (int)((unsigned)y1 & mask) - half;
-        y0 >>= bits;
-        y1 >>= bits;
-      }
+    for (int pos = 0; pos < NS - 1; ++pos) {
+      const uint32_t b = __byte_perm(word(Y0, pos >> 2), word(Y1, pos >> 2), (pos & 3) | ((4 + (pos & 3)) << 8));
+      const uint32_t w = ((b & 0x00ff00ffu) ^ flip) + add;
+      *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
+      o -= plane_elems;
+    }
+    {
+      // top digit: the remaining bits, in [0, 2^bits]
+      const int d0 = (int)(unsigned)(Y0 >> (bits * (NS - 1))), d1 = (int)(unsigned)(Y1 >> (bits * (NS - 1)));
       const unsigned u0 = (unsigned)((n0 ? -d0 : d0) + (1 << bits)), u1 = (unsigned)((n1 ? -d1 : d1) + (1 << bits));
       const unsigned w = 0x64006400u | u0 | (u1 << 16);
       *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
-      o -= plane_elems;
     }
   }
 };
