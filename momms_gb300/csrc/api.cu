@@ -40,8 +40,16 @@ cudaError_t device_malloc(void** ptr, size_t bytes) {
   return cudaMalloc(ptr, bytes);
 }
 
+namespace {
+thread_local cudaError_t g_refused_launch = cudaSuccess;
+}  // namespace
+
+void refuse_launch(cudaError_t e) { g_refused_launch = e; }
+
 cudaError_t launch_status() {
   cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && g_refused_launch != cudaSuccess) e = g_refused_launch;
+  g_refused_launch = cudaSuccess;
   if (e == cudaSuccess && fault_take(MOMMS_FAULT_CUDA)) e = cudaErrorLaunchFailure;
   return e;
 }

@@ -58,6 +58,9 @@ DeviceState* device_state();
 bool fault_take(int kind);
 cudaError_t device_malloc(void** ptr, size_t bytes);
 cudaError_t launch_status();
+// A launcher that declines to launch (arguments its kernel cannot take)
+// records the error here; the next launch_status() on this thread returns it.
+void refuse_launch(cudaError_t e);
 
 // Record an error message for momms_last_error() and return `code`.
 int fail(int code, const char* fmt, ...);

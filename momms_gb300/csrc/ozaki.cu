@@ -41,7 +41,6 @@
 #include "slicegemm.cuh"
 
 namespace momms {
-
 namespace {
 
 constexpr int kDigitBits = 8;
@@ -64,9 +63,13 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-// Row maxima of |x(r, p)| as bit patterns. A block covers 32 rows x 256 of p,
-// reads along whichever index is contiguous, reduces in registers / shared
-// memory and posts one atomicMax per row (maxbits must start at zero).
+// Row maxima of |x(r, p)| as bit patterns, rows contiguous (a column-major
+// A). A block covers 32 rows x 256 of p, reads along r with all of a thread's
+// 32 loads issued before the first maximum, reduces in registers / shared
+// memory and posts one atomicMax per row (maxbits must start at zero). At
+// 8192^2 this reads at 4.8 TB/s (108 us), against 3.8 for the run layout of
+// the other prep kernels (133 us); with p contiguous the run layout is the
+// faster one (132 us, against 230 for this kernel's lanes-along-p branch).
 __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
                                                          int64_t R, int64_t K, bool r_contig,
                                                          unsigned long long* __restrict__ maxbits) {
@@ -89,8 +92,7 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restric
       if (mx) atomicMax(&maxbits[r], mx);
     }
   } else {
-    // one warp per row, lanes along p; all 32 loads of a thread in flight
-    // before the first maximum
+    // one warp per row, lanes along p
     double v[4][8];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -111,6 +113,37 @@ __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restric
       for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       if (tx == 0 && mx && r < R) atomicMax(&maxbits[r], mx);
     }
+  }
+}
+
+// Row maxima with p contiguous (or general strides), in the run layout of
+// planes.cuh: the lanes of one row reduce by shuffles and one posts an
+// atomicMax (maxbits must start at zero).
+__global__ void __launch_bounds__(planes::THREADS)
+    row_absmax_runs_kernel(const double* __restrict__ x, int64_t sr, int64_t sp, int64_t R, int64_t K, bool vec,
+                           int lg, unsigned long long* __restrict__ maxbits) {
+  constexpr int RUN = 8;
+  const planes::Chunk<false> c(lg);
+  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * planes::PITER;
+  // the row loop's trip count is the same for every thread of the block, so
+  // every lane reaches the shuffles
+  for (int64_t rb = (int64_t)blockIdx.y * c.rows; rb < R; rb += (int64_t)gridDim.y * c.rows) {
+    const int64_t r = rb + c.rl;
+    unsigned long long mx = 0;
+    if (r < R) {
+      const double* xr = x + r * sr;
+#pragma unroll 1
+      for (int it = 0; it < planes::PITER; ++it) {
+        const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+        if (p >= K) break;
+        double v[RUN];
+        planes::load_run<false, RUN>(xr, sp, p, K, vec, v);
+#pragma unroll
+        for (int i = 0; i < RUN; ++i) mx = max(mx, abs_bits(v[i]));
+      }
+    }
+    for (int o = c.runs >> 1; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (c.ru == 0 && r < R && mx) atomicMax(&maxbits[r], mx);
   }
 }
 
@@ -169,15 +202,18 @@ __device__ __forceinline__ U offset_digits(double v, int e) {
 // does).
 template <int NS>
 struct OzakiSliceOp {
+  static constexpr int PLANES = NS;
   using Tout = __half;
+  using Word = uint32_t;  // one pair's __half2 bits
   using U = typename std::conditional<(kDigitBits * NS <= 62), unsigned long long, unsigned __int128>::type;
   const int* exps;
+  __device__ __forceinline__ int row(int64_t r) const { return exps[r]; }
   // 32-bit word w of Y
   __device__ __forceinline__ static uint32_t word(U y, int w) { return (uint32_t)(y >> (32 * w)); }
-  __device__ __forceinline__ void pair(double v0, double v1, int64_t r, __half* out, int64_t plane_elems) const {
+  __device__ __forceinline__ static uint32_t bits_of(__half2 h) { return *reinterpret_cast<const uint32_t*>(&h); }
+  __device__ __forceinline__ void pack(double v0, double v1, int e, uint32_t (&out)[NS]) const {
     constexpr int bits = kDigitBits;
     static_assert(bits == 8, "lower digits are the bytes of Y");
-    const int e = exps[r];
     const U Y0 = offset_digits<NS, U>(v0, e), Y1 = offset_digits<NS, U>(v1, e);
     const bool n0 = __double_as_longlong(v0) < 0, n1 = __double_as_longlong(v1) < 0;
     static_assert(2 * (1 << bits) < 1024, "digits must fit the 0x6400 pattern");
@@ -188,21 +224,19 @@ struct OzakiSliceOp {
     // for both elements of the pair at once, bytes in 16-bit lanes 0 and 1.
     const uint32_t flip = (n0 ? 0xffu : 0u) | (n1 ? 0xff0000u : 0u);
     const uint32_t add = 0x64006400u + ((n0 ? 129u : 128u) | ((n1 ? 129u : 128u) << 16));
-    // least significant position first, into the last plane, walking back
-    __half* o = out + (int64_t)(NS - 1) * plane_elems;
+    // digit position pos goes to plane NS-1-pos
 #pragma unroll
     for (int pos = 0; pos < NS - 1; ++pos) {
       const uint32_t b = __byte_perm(word(Y0, pos >> 2), word(Y1, pos >> 2), (pos & 3) | ((4 + (pos & 3)) << 8));
       const uint32_t w = ((b & 0x00ff00ffu) ^ flip) + add;
-      *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
-      o -= plane_elems;
+      out[NS - 1 - pos] = bits_of(__hsub2(*reinterpret_cast<const __half2*>(&w), bias));
     }
     {
       // top digit: the remaining bits, in [0, 2^bits]
       const int d0 = (int)(unsigned)(Y0 >> (bits * (NS - 1))), d1 = (int)(unsigned)(Y1 >> (bits * (NS - 1)));
       const unsigned u0 = (unsigned)((n0 ? -d0 : d0) + (1 << bits)), u1 = (unsigned)((n1 ? -d1 : d1) + (1 << bits));
       const unsigned w = 0x64006400u | u0 | (u1 << 16);
-      *reinterpret_cast<__half2*>(o) = __hsub2(*reinterpret_cast<const __half2*>(&w), bias);
+      out[0] = bits_of(__hsub2(*reinterpret_cast<const __half2*>(&w), bias));
     }
   }
 };
@@ -566,10 +600,22 @@ int ozaki_operand_exponents(const double* x, int64_t sr, int64_t sp, int64_t R, 
   KernelTimer kt(MOMMS_KERNEL_PREP, s);
   cudaError_t ce = cudaMemsetAsync(maxbits, 0, (size_t)R * sizeof(unsigned long long), s);
   if (ce != cudaSuccess) return cuda_fail(ce, "Ozaki exponents");
-  row_absmax_kernel<<<dim3((unsigned)ceil_div(K, 256), (unsigned)ceil_div(R, 32)), dim3(32, 8), 0, s>>>(
-      x, sr, sp, R, K, r_contig, maxbits);
+  int launches = 1;
+  if (r_contig) {
+    // rows in launches of at most 65535 row tiles (the grid's y limit)
+    for (int64_t rb = 0; rb < R; rb += (int64_t)65535 * 32, ++launches) {
+      const int64_t rn = std::min<int64_t>(R - rb, (int64_t)65535 * 32);
+      row_absmax_kernel<<<dim3((unsigned)ceil_div(K, 256), (unsigned)ceil_div(rn, 32)), dim3(32, 8), 0, s>>>(
+          x + rb * sr, sr, sp, rn, K, true, maxbits + rb);
+    }
+  } else {
+    const int lg = planes::run_lanes_log2(K, 8, false, planes::kRowsContigLg);
+    row_absmax_runs_kernel<<<planes::run_grid<false, 8>(R, K, lg), planes::THREADS, 0, s>>>(
+        x, sr, sp, R, K, planes::rows_vector_aligned(x, sr, sp), lg, maxbits);
+    ++launches;
+  }
   exps_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, s>>>(maxbits, R, exps);
-  note_launch(2);
+  note_launch(launches);
   ce = launch_status();
   return ce == cudaSuccess ? MOMMS_OK : cuda_fail(ce, "Ozaki exponents");
 }
@@ -878,47 +924,57 @@ __device__ __forceinline__ void magnitude(double v, int e, bool indicator, uint1
 }
 
 // Magnitude plane and row sums of an R x K view (element (r, p) at
-// x[r*sr + p*sp]) under the row exponents: a block stages 32 rows x 64 of p
-// (coalesced along whichever index is contiguous), then each warp converts
-// one row's 64 elements (a lane per pair), sums the fixed-point terms over the
-// warp and posts one 64-bit atomicAdd (exact, so the sums do not depend on
-// timing). With `indicator` it writes the 0/1 plane of nonzero elements and
-// no sums.
+// x[r*sr + p*sp]) under the row exponents, in the run layout of planes.cuh:
+// a thread converts runs of 8 elements of one row (one 16-byte store of bf16
+// each) and adds their fixed-point terms in a register; the lanes of one
+// row (4, or 2^lg) add their terms by shuffles and one of them posts a 64-bit
+// atomicAdd. The sums are exact integers, so they do not depend on the order
+// of the atomics. With `indicator` the kernel writes the 0/1 plane of nonzero
+// elements and no sums.
 template <bool R_CONTIG>
-__global__ void __launch_bounds__(256) magnitude_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
-                                                        int64_t R, int64_t K, const int* __restrict__ exps,
-                                                        uint16_t* __restrict__ plane, int64_t ldp,
-                                                        unsigned long long* __restrict__ sums, bool indicator) {
-  constexpr int TR = planes::TILE_R, TP = planes::TILE_P;
-  static_assert(planes::THREADS == 256, "one warp per 8th row of the tile");
-  __shared__ double tile[TR][TP + 1];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t p0 = (int64_t)blockIdx.x * TP;
-  const int64_t pp = p0 + 2 * lane;
-  for (int64_t r0 = (int64_t)blockIdx.y * TR; r0 < R; r0 += (int64_t)gridDim.y * TR) {
-    __syncthreads();
-    planes::stage_tile<R_CONTIG>(x, sr, sp, R, K, r0, p0, tile);
-    __syncthreads();
-    uint16_t* out = plane + (r0 + warp) * ldp + pp;
-#pragma unroll 1
-    for (int rl = warp; rl < TR; rl += 8, out += 8 * ldp) {
-      const int64_t r = r0 + rl;
-      if (r >= R) break;  // uniform over the warp
+__global__ void __launch_bounds__(planes::THREADS)
+    magnitude_kernel(const double* __restrict__ x, int64_t sr, int64_t sp, int64_t R, int64_t K, bool vec, int lg,
+                     const int* __restrict__ exps, uint16_t* __restrict__ plane, int64_t ldp,
+                     unsigned long long* __restrict__ sums, bool indicator) {
+  constexpr int RUN = 8;
+  const planes::Chunk<R_CONTIG> c(lg);
+  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * planes::PITER;
+  // the row loop's trip count is the same for every thread of the block
+  // (rows past R only skip their work), so every lane reaches the shuffles
+  for (int64_t rb = (int64_t)blockIdx.y * c.rows; rb < R; rb += (int64_t)gridDim.y * c.rows) {
+    const int64_t r = rb + c.rl;
+    unsigned long long t = 0;
+    if (r < R) {
       const int e = exps[r];
-      uint16_t b0 = 0, b1 = 0;
-      unsigned long long f0 = 0, f1 = 0;
-      if (pp < K) {
-        magnitude(tile[rl][2 * lane], e, indicator, &b0, &f0);
-        magnitude(tile[rl][2 * lane + 1], e, indicator, &b1, &f1);  // beyond K: the tile holds 0
-        *reinterpret_cast<unsigned*>(out) = (unsigned)b0 | ((unsigned)b1 << 16);
-      }
-      if (!indicator) {
-        unsigned long long t = f0 + f1;
+      const double* xr = x + r * sr;
+      uint16_t* outr = plane + r * ldp;
+#pragma unroll 1
+      for (int it = 0; it < planes::PITER; ++it) {
+        const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+        if (p >= K) break;
+        double v[RUN];
+        planes::load_run<R_CONTIG, RUN>(xr, sp, p, K, vec, v);
+        uint32_t w[RUN / 2];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0 && t) atomicAdd(&sums[r], t);
+        for (int q = 0; q < RUN / 2; ++q) {
+          uint16_t b0, b1;
+          unsigned long long f0, f1;
+          magnitude(v[2 * q], e, indicator, &b0, &f0);
+          magnitude(v[2 * q + 1], e, indicator, &b1, &f1);
+          w[q] = (uint32_t)b0 | ((uint32_t)b1 << 16);
+          t += f0 + f1;
+        }
+        *reinterpret_cast<uint4*>(outr + p) = make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
+    if (indicator) continue;
+    // a row's lanes differ in the top lg lane bits (rows contiguous) or in the low lg bits
+    if (R_CONTIG) {
+      for (int o = 16; o >= (32 >> lg); o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    } else {
+      for (int o = c.runs >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    if (c.ru == 0 && r < R && t) atomicAdd(&sums[r], t);
   }
 }
 
@@ -926,11 +982,18 @@ int enqueue_magnitudes(const double* x, int64_t sr, int64_t sp, int64_t R, int64
                        uint16_t* plane, int64_t kp, unsigned long long* sums, cudaStream_t s, bool indicator = false) {
   if (R == 0) return MOMMS_OK;
   const bool r_contig = (sr == 1 && sp != 1);
-  dim3 grid((unsigned)ceil_div(K, 64), (unsigned)std::min<int64_t>(ceil_div(R, 32), 65535));
+  const bool vec = planes::rows_vector_aligned(x, sr, sp);
+  if (kp % 8 || (reinterpret_cast<uintptr_t>(plane) & 15))
+    return fail(MOMMS_ERR_INVALID_ARG, "Ozaki bound magnitudes: plane rows not 16-byte aligned");
+  const int lg = planes::run_lanes_log2(K, 8, r_contig, planes::kRowsContigLg);
   {
     KernelTimer kt(MOMMS_KERNEL_PREP, s);
-    if (r_contig) magnitude_kernel<true><<<grid, 256, 0, s>>>(x, sr, sp, R, K, exps, plane, kp, sums, indicator);
-    else magnitude_kernel<false><<<grid, 256, 0, s>>>(x, sr, sp, R, K, exps, plane, kp, sums, indicator);
+    if (r_contig)
+      magnitude_kernel<true><<<planes::run_grid<true, 8>(R, K, lg), planes::THREADS, 0, s>>>(
+          x, sr, sp, R, K, vec, lg, exps, plane, kp, sums, indicator);
+    else
+      magnitude_kernel<false><<<planes::run_grid<false, 8>(R, K, lg), planes::THREADS, 0, s>>>(
+          x, sr, sp, R, K, vec, lg, exps, plane, kp, sums, indicator);
   }
   note_launch();
   const cudaError_t e = launch_status();

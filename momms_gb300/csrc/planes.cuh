@@ -3,86 +3,174 @@
 // An operand is viewed as R x K (A: R = m; B transposed: R = n), element
 // (r, p) at x[r*sr + p*sp]. Each element is split by `Op` into values written
 // to planes[t][r][p] (p contiguous, row stride ldp, plane stride
-// plane_elems). A block stages a 32 x 64 tile in shared memory so that the
-// read (along whichever index is contiguous in the source) and the write
-// (along p) are both coalesced; each thread then splits two neighbouring
-// elements of a row and stores each plane's pair as one vector (a warp writes
-// 128 contiguous bytes of fp16 per plane). Requires ldp and plane_elems even
-// and `planes` 8-byte aligned; the pair at the end of an odd K covers a
-// padding column (p = K <= ldp - 1), which receives the split of zero.
+// plane_elems).
+//
+// Work is cut into runs: RUN consecutive elements of one row, RUN * sizeof
+// of the plane type = 16 bytes, so that a run's values of one plane leave in
+// one vector store. The warp layout follows the source's contiguous index:
+//   * rows contiguous (a column-major A): a warp takes 8 consecutive rows x
+//     4 consecutive runs (lane = 8 * run + row), so each of a thread's RUN
+//     loads reads four 64-byte pieces (8 rows of 4 columns) and each plane
+//     store writes 64 contiguous bytes (4 runs) of each of 8 rows: whole
+//     32-byte sectors. (With a warp on 32 rows of one run, every store was 32
+//     separate 16-byte pieces, one L2 write request each, and the digit pass
+//     was store-throttled.);
+//   * otherwise (p contiguous, or general strides): the lanes take 32
+//     consecutive runs of one row, read with 16-byte vector loads where the
+//     row is aligned, and each plane store is one contiguous 512-byte warp
+//     access. Rows shorter than 32 runs share a warp: 2^lg lanes per row,
+//     2^lg the smallest power of two covering the row's runs.
+// Nothing goes through shared memory and nothing waits at a barrier. A
+// thread converts PITER runs of its row (PITER warp-widths apart along p).
+// (Loading the next run while converting the current one took more
+// registers than it hid latency: 0.277 -> 0.284 ms for the digits of A,
+// 0.14 -> 0.17 ms for the magnitudes, at 8192^2.)
+// Requires ldp, plane_elems and the plane base aligned to RUN elements
+// (16 bytes); the last run of a row may extend past K up to
+// round_up(K, RUN) <= ldp, and those padding columns receive the split of zero.
 #pragma once
 #include "common.cuh"
 
 namespace momms {
+void refuse_launch(cudaError_t e);
 namespace planes {
 
-constexpr int TILE_R = 32, TILE_P = 64, THREADS = 256;
+constexpr int THREADS = 256, PITER = 4;
 
-// Stages rows r0..r0+31, columns p0..p0+63 of the view into tile (zeros
-// outside it). Every thread's element of pass i lies a fixed distance from
-// its element of pass 0 (8 columns on when rows are contiguous, 4 rows on
-// otherwise), so a pass costs one pointer step; interior tiles skip the
-// bounds checks.
-template <bool R_CONTIG, typename Tin>
-__device__ __forceinline__ void stage_tile(const Tin* __restrict__ x, int64_t sr, int64_t sp, int64_t R, int64_t K,
-                                           int64_t r0, int64_t p0, Tin (&tile)[TILE_R][TILE_P + 1]) {
-  const int tid = threadIdx.x;
-  // pass i: rows-contiguous (rl, pl) = (tid % 32, tid / 32 + 8 i), else (tid / 64 + 4 i, tid % 64)
-  const int rl0 = R_CONTIG ? (tid % TILE_R) : (tid / TILE_P);
-  const int pl0 = R_CONTIG ? (tid / TILE_R) : (tid % TILE_P);
-  constexpr int DR = R_CONTIG ? 0 : THREADS / TILE_P, DP = R_CONTIG ? THREADS / TILE_R : 0;
-  const Tin* q = x + (r0 + rl0) * sr + (p0 + pl0) * sp;
-  const int64_t step = R_CONTIG ? (int64_t)DP * sp : (int64_t)DR * sr;
-  constexpr int PASSES = TILE_R * TILE_P / THREADS;
-  if (r0 + TILE_R <= R && p0 + TILE_P <= K) {
-    Tin v[PASSES];
+// A thread's place in a block's chunk of the view: row rl of the chunk's
+// rows, run ru of the runs taken across the chunk per iteration. A warp
+// holds 32 >> lg rows of 2^lg runs each; rows contiguous: consecutive lanes
+// take consecutive rows (lane = run * rows_per_warp + row), otherwise
+// consecutive runs of a row.
+template <bool R_CONTIG>
+struct Chunk {
+  int rows, runs, rl, ru;
+  __device__ __forceinline__ explicit Chunk(int lg) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (R_CONTIG) {
+      const int rpw = 32 >> lg;
+      rows = (THREADS / 32) * rpw, runs = 1 << lg, rl = warp * rpw + (lane & (rpw - 1)), ru = lane >> (5 - lg);
+    } else {
+      rows = (THREADS / 32) << (5 - lg), runs = 1 << lg;
+      rl = (warp << (5 - lg)) + (lane >> lg), ru = lane & (runs - 1);
+    }
+  }
+};
+
+// Lanes per row (log2) for rows of K elements in runs of RUN: rows not
+// contiguous, the smallest power of two covering the row's runs (at most
+// 32); rows contiguous, `rows_contig_lg` capped the same way.
+inline int run_lanes_log2(int64_t K, int run, bool r_contig, int rows_contig_lg) {
+  const int64_t runs = (K + run - 1) / run;
+  int lg = 0;
+  while (lg < 5 && ((int64_t)1 << lg) < runs) ++lg;
+  return r_contig ? std::min(lg, rows_contig_lg) : lg;
+}
+// Rows-contiguous lanes per row (log2) of the prep kernels: 4 runs of a row
+// per warp, 8 rows (measured at 8192^2 digits: 0.28 ms, against 0.35 ms for
+// 16 rows x 2 runs and 1.02 ms for 32 rows x 1 run, whose 16-byte row pieces
+// cost one L2 write request each).
+constexpr int kRowsContigLg = 2;
+
+// Loads the run of row xr starting at p (p a multiple of RUN): RUN elements,
+// zeros past K. `vec`: p contiguous and the row 16-byte aligned, so the run
+// is read with 16-byte vector loads.
+template <bool R_CONTIG, int RUN, typename Tin>
+__device__ __forceinline__ void load_run(const Tin* __restrict__ xr, int64_t sp, int64_t p, int64_t K, bool vec,
+                                         Tin (&v)[RUN]) {
+  static_assert((RUN * sizeof(Tin)) % 16 == 0, "a run is whole 16-byte vectors");
+  if (p + RUN <= K) {
+    if (!R_CONTIG && vec) {
+      const uint4* q = reinterpret_cast<const uint4*>(xr + p);
+      uint4 t[RUN * sizeof(Tin) / 16];
 #pragma unroll
-    for (int i = 0; i < PASSES; ++i) v[i] = q[i * step];
+      for (int i = 0; i < RUN * (int)sizeof(Tin) / 16; ++i) t[i] = __ldg(q + i);
+      memcpy(v, t, sizeof(v));
+    } else {
+      const Tin* q = xr + p * sp;
 #pragma unroll
-    for (int i = 0; i < PASSES; ++i) tile[rl0 + DR * i][pl0 + DP * i] = v[i];
+      for (int i = 0; i < RUN; ++i) v[i] = __ldg(q + i * sp);
+    }
   } else {
 #pragma unroll
-    for (int i = 0; i < PASSES; ++i) {
-      const int rl = rl0 + DR * i, pl = pl0 + DP * i;
-      tile[rl][pl] = (r0 + rl < R && p0 + pl < K) ? q[i * step] : Tin(0);
+    for (int i = 0; i < RUN; ++i) v[i] = (p + i < K) ? __ldg(xr + (p + i) * sp) : Tin(0);
+  }
+}
+
+// Op: PLANES, Tout, Word (one pair's value in one plane: two Tout), Ctx
+// row(r) (per-row state) and pack(v0, v1, ctx, Word (&w)[PLANES]).
+template <bool R_CONTIG, typename Tin, typename Op>
+__global__ void __launch_bounds__(THREADS)
+    to_planes_kernel(const Tin* __restrict__ x, int64_t sr, int64_t sp, int64_t R, int64_t K, bool vec, int lg,
+                     typename Op::Tout* __restrict__ planes, int64_t ldp, int64_t plane_elems, Op op) {
+  using Tout = typename Op::Tout;
+  using Word = typename Op::Word;
+  constexpr int RUN = 16 / sizeof(Tout), NP = Op::PLANES;
+  static_assert(sizeof(Word) == 2 * sizeof(Tout), "a word is one pair's value");
+  const Chunk<R_CONTIG> c(lg);
+  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * PITER;
+  // row chunks beyond the grid's y limit are taken in further passes
+  for (int64_t r = (int64_t)blockIdx.y * c.rows + c.rl; r < R; r += (int64_t)gridDim.y * c.rows) {
+    const auto ctx = op.row(r);
+    const Tin* xr = x + r * sr;
+    Tout* outr = planes + r * ldp;
+#pragma unroll 1
+    for (int it = 0; it < PITER; ++it) {
+      const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+      if (p >= K) break;
+      Tin v[RUN];
+      load_run<R_CONTIG, RUN>(xr, sp, p, K, vec, v);
+      Word w[NP][RUN / 2];
+#pragma unroll
+      for (int q = 0; q < RUN / 2; ++q) {
+        Word wq[NP];
+        op.pack(v[2 * q], v[2 * q + 1], ctx, wq);
+#pragma unroll
+        for (int t = 0; t < NP; ++t) w[t][q] = wq[t];
+      }
+#pragma unroll
+      for (int t = 0; t < NP; ++t) {
+        uint4 u;
+        memcpy(&u, w[t], sizeof(u));
+        *reinterpret_cast<uint4*>(outr + t * plane_elems + p) = u;
+      }
     }
   }
 }
 
-template <bool R_CONTIG, typename Tin, typename Op>
-__global__ void __launch_bounds__(THREADS, 4)
-    to_planes_kernel(const Tin* __restrict__ x, int64_t sr, int64_t sp, int64_t R, int64_t K,
-                     typename Op::Tout* __restrict__ planes, int64_t ldp, int64_t plane_elems, Op op) {
-  __shared__ Tin tile[TILE_R][TILE_P + 1];
-  const int tid = threadIdx.x;
-  const int64_t p0 = (int64_t)blockIdx.x * TILE_P;
-  // a thread splits the pair at column 2 (tid % 32) of rows tid / 32 + 8 i
-  const int pr = tid % (TILE_P / 2), rl0 = tid / (TILE_P / 2);
-  const int64_t pp = p0 + 2 * pr;
-  // row tiles beyond the grid's y limit are taken in further passes
-  for (int64_t r0 = (int64_t)blockIdx.y * TILE_R; r0 < R; r0 += (int64_t)gridDim.y * TILE_R) {
-    __syncthreads();  // the previous pass's readers are done with the tile
-    stage_tile<R_CONTIG>(x, sr, sp, R, K, r0, p0, tile);
-    __syncthreads();
-    if (pp >= K) continue;
-    typename Op::Tout* out = planes + (r0 + rl0) * ldp + pp;
-#pragma unroll 1
-    for (int i = 0; i < TILE_R * (TILE_P / 2) / THREADS; ++i) {
-      const int rl = rl0 + (THREADS / (TILE_P / 2)) * i;
-      if (r0 + rl >= R) break;
-      op.pair(tile[rl][2 * pr], tile[rl][2 * pr + 1], r0 + rl, out, plane_elems);
-      out += (int64_t)(THREADS / (TILE_P / 2)) * ldp;
-    }
-  }
+// Grid of a run kernel over an R x K view (lg: run_lanes_log2, used when
+// rows are not contiguous).
+template <bool R_CONTIG, int RUN>
+inline dim3 run_grid(int64_t R, int64_t K, int lg) {
+  const int64_t rows = (int64_t)(THREADS / 32) << (5 - lg);
+  const int64_t runs = (int64_t)1 << lg;
+  return dim3((unsigned)ceil_div_dev(K, runs * RUN * PITER), (unsigned)std::min<int64_t>(ceil_div_dev(R, rows), 65535));
+}
+
+// True when row r of the view starts 16-byte aligned for every r and p is
+// contiguous, so that runs may be read as vectors.
+template <typename Tin>
+inline bool rows_vector_aligned(const Tin* x, int64_t sr, int64_t sp) {
+  return sp == 1 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 && ((sr * (int64_t)sizeof(Tin)) & 15) == 0;
 }
 
 template <typename Tin, typename Op>
 void launch_to_planes(const Tin* x, int64_t sr, int64_t sp, int64_t R, int64_t K, typename Op::Tout* planes,
                       int64_t ldp, int64_t plane_elems, Op op, cudaStream_t s) {
+  constexpr int RUN = 16 / sizeof(typename Op::Tout);
+  if (ldp % RUN || plane_elems % RUN || (reinterpret_cast<uintptr_t>(planes) & 15)) {
+    refuse_launch(cudaErrorMisalignedAddress);  // the vector stores need 16-byte aligned runs
+    return;
+  }
   const bool r_contig = (sr == 1 && sp != 1);
-  dim3 grid((unsigned)ceil_div_dev(K, TILE_P), (unsigned)std::min<int64_t>(ceil_div_dev(R, TILE_R), 65535));
-  if (r_contig) to_planes_kernel<true, Tin, Op><<<grid, THREADS, 0, s>>>(x, sr, sp, R, K, planes, ldp, plane_elems, op);
-  else to_planes_kernel<false, Tin, Op><<<grid, THREADS, 0, s>>>(x, sr, sp, R, K, planes, ldp, plane_elems, op);
+  const bool vec = rows_vector_aligned(x, sr, sp);
+  const int lg = run_lanes_log2(K, RUN, r_contig, kRowsContigLg);
+  if (r_contig)
+    to_planes_kernel<true, Tin, Op>
+        <<<run_grid<true, RUN>(R, K, lg), THREADS, 0, s>>>(x, sr, sp, R, K, vec, lg, planes, ldp, plane_elems, op);
+  else
+    to_planes_kernel<false, Tin, Op>
+        <<<run_grid<false, RUN>(R, K, lg), THREADS, 0, s>>>(x, sr, sp, R, K, vec, lg, planes, ldp, plane_elems, op);
 }
 
 }  // namespace planes

@@ -15,7 +15,10 @@ namespace momms {
 
 namespace {
 struct Tf32SplitOp {
+  static constexpr int PLANES = 2;  // hi, lo
   using Tout = float;
+  using Word = uint2;  // one pair's float2 bits
+  __device__ __forceinline__ int row(int64_t) const { return 0; }
   __device__ __forceinline__ static void split(float v, float* hi_out, float* lo_out) {
     uint32_t hi, lo;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(v));
@@ -24,13 +27,13 @@ struct Tf32SplitOp {
     *hi_out = __uint_as_float(hi);
     *lo_out = __uint_as_float(lo);
   }
-  // two neighbouring elements of a row: one 8-byte store per plane
-  __device__ __forceinline__ void pair(float v0, float v1, int64_t, float* out, int64_t plane_elems) const {
-    float2 hi, lo;
-    split(v0, &hi.x, &lo.x);
-    split(v1, &hi.y, &lo.y);
-    *reinterpret_cast<float2*>(out) = hi;
-    *reinterpret_cast<float2*>(out + plane_elems) = lo;
+  // two neighbouring elements of a row: their hi pair and lo pair
+  __device__ __forceinline__ void pack(float v0, float v1, int, uint2 (&out)[2]) const {
+    float h0, h1, l0, l1;
+    split(v0, &h0, &l0);
+    split(v1, &h1, &l1);
+    out[0] = make_uint2(__float_as_uint(h0), __float_as_uint(h1));
+    out[1] = make_uint2(__float_as_uint(l0), __float_as_uint(l1));
   }
 };
 }  // namespace
