@@ -167,13 +167,27 @@ __device__ __forceinline__ void drain_chunk(uint32_t taddr, EpiAcc<EPI> (&S)[NC]
 // and posted to the two maxima. Every lane calls it (rows past m contribute 0).
 template <int NC>
 __device__ __forceinline__ void bound_tile(const Params& p, int64_t row, int64_t col0, const float (&S)[NC]) {
+  static_assert(NC % 32 == 0, "columns are shared out 32 per lane round");
   float m1 = 0.0f, m2 = 0.0f;
   unsigned cnt = 0;
-  if (row < p.m && p.count_only) {
+  // columns of this tile inside C (the same for the whole warp)
+  const int nvalid = (int)min((int64_t)NC, max((int64_t)0, p.n - col0));
+  if (p.count_only) {
+    if (row < p.m) {
 #pragma unroll
-    for (int j = 0; j < NC; ++j) cnt += (col0 + j < p.n && S[j] > 0.0f) ? 1u : 0u;
-  } else if (row < p.m) {
-    const float sa = __fmul_ru(__ull2float_ru(p.msum_a[row]), 0x1p-40f);
+      for (int j = 0; j < NC; ++j) cnt += (j < nvalid && S[j] > 0.0f) ? 1u : 0u;
+    }
+  } else {
+    // The warp's 32 rows share their NC columns: each lane converts the
+    // column sums of every 32nd column once (upward, units of 2^-40) and the
+    // entries take them by shuffle.
+    const int lane = threadIdx.x & 31;
+    float sbl[NC / 32];
+#pragma unroll
+    for (int q = 0; q < NC / 32; ++q)
+      sbl[q] = 32 * q + lane < nvalid ? __fmul_ru(__ull2float_ru(p.msum_b[col0 + 32 * q + lane]), 0x1p-40f) : 0.0f;
+    const bool rv = row < p.m;
+    const float sa = rv ? __fmul_ru(__ull2float_ru(p.msum_a[row]), 0x1p-40f) : 0.0f;
     // q2 = k / L needs only the row's smallest L: one reciprocal per row.
     // q1 = (sa + sb) / L: an entry whose (sa + sb), rounded up, is at most
     // m1 * L rounded down cannot raise m1 (its quotient is at most m1), so
@@ -181,14 +195,14 @@ __device__ __forceinline__ void bound_tile(const Params& p, int64_t row, int64_t
     float lmin = INFINITY;
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
-      const int64_t col = col0 + j;
+      const float sb = __shfl_sync(0xffffffffu, sbl[j >> 5], j & 31);
       const float lb = __fmul_rd(S[j], p.lb_scale);
       // L = 0: no p with both a_ip and b_pj nonzero (the entry has no
       // error), or every term below FP32's range: counted, the host tells
       // the two apart
-      if (col < p.n) {
+      if (rv && j < nvalid) {
         if (lb > 0.0f) {
-          const float x = __fadd_ru(sa, __fmul_ru(__ull2float_ru(p.msum_b[col]), 0x1p-40f));
+          const float x = __fadd_ru(sa, sb);
           if (x > __fmul_rd(m1, lb)) m1 = fmaxf(m1, __fmul_ru(x, __frcp_ru(lb)));
           lmin = fminf(lmin, lb);
         } else {
