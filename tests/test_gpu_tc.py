@@ -208,3 +208,65 @@ def test_no_bounded_wait_expired(gpu):
     bits = ctypes.c_uint32(0)
     assert gpu.momms_device_status(ctypes.byref(bits)) == mg.OK, bits.value
     assert bits.value == 0
+
+
+# ------------------------------------------------------- operand passes, layouts
+def _device_view(X, kind, rng):
+    """A device tensor holding X's values in the given layout: "col" / "row"
+    (contiguous), "offset" (a view one element past an aligned start, leading
+    dimension odd: rows never 16-byte aligned), "strided" (neither stride 1)."""
+    import torch
+    r, c = X.shape
+    t = torch.from_numpy(np.ascontiguousarray(X))
+    if kind == "col":
+        return t.t().contiguous().t().cuda()
+    if kind == "row":
+        return t.cuda()
+    if kind == "offset":
+        ld = r + 3 if (r + 3) % 2 else r + 4
+        big = torch.zeros((c * ld + 1,), dtype=t.dtype).cuda()
+        v = torch.as_strided(big, (r, c), (1, ld), storage_offset=1)
+        v.copy_(t.cuda())
+        return v
+    if kind == "strided":
+        big = torch.zeros((2 * r, 3 * c), dtype=t.dtype).cuda()
+        v = big[::2, ::3]
+        v.copy_(t.cuda())
+        return v
+    raise ValueError(kind)
+
+
+def _run_views(lib, A, B, C0, prec, a_kind, b_kind):
+    import ctypes
+    import torch
+    m, k = A.shape
+    n = B.shape[1]
+    dt = mg.DTYPE_F64 if A.dtype == np.float64 else mg.DTYPE_F32
+    ta, tb = _device_view(A, a_kind, None), _device_view(B, b_kind, None)
+    tc = torch.from_numpy(np.asfortranarray(C0).T.copy()).cuda().t()  # column-major C
+    d = gu.make_desc(dt, m, n, k, 0.5, -1.0, (ta.data_ptr(), ta.stride(0), ta.stride(1)),
+                     (tb.data_ptr(), tb.stride(0), tb.stride(1)), (tc.data_ptr(), tc.stride(0), tc.stride(1)),
+                     precision=prec)
+    mg.check(lib.momms_gemm(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), lib)
+    torch.cuda.synchronize()
+    return tc.cpu().numpy()
+
+
+@pytest.mark.parametrize("prec", [mg.PREC_OZAKI, mg.PREC_SPLIT_TF32])
+@pytest.mark.parametrize("shape", [(257, 190, 203), (300, 45, 5), (7000, 40, 24)])
+def test_operand_passes_layout_independent(gpu, prec, shape):
+    """Row maxima, magnitudes and digit planes depend only on the values, so
+    the result is bit-identical whatever layout the operands arrive in: rows
+    contiguous or not, rows not 16-byte aligned (scalar loads), neither
+    stride 1, rows of a few elements (several rows per warp), many rows."""
+    rng = np.random.default_rng(hash(shape) % 2**32)
+    m, n, k = shape
+    dt = np.float64 if prec == mg.PREC_OZAKI else np.float32
+    A, B, C0 = _mats(rng, m, n, k, dt)
+    ref = _run_views(gpu, A, B, C0, prec, "col", "col")
+    for a_kind, b_kind in [("row", "row"), ("offset", "offset"), ("strided", "strided"), ("row", "offset"),
+                           ("offset", "strided")]:
+        C = _run_views(gpu, A, B, C0, prec, a_kind, b_kind)
+        assert np.array_equal(C, ref), (a_kind, b_kind)
+    exact, mag = ou.dd_gemm(A.astype(np.float64), B.astype(np.float64), C0.astype(np.float64), alpha=0.5, beta=-1.0)
+    assert ou.bound_ratio(ref, exact, mag, k, U64 if dt == np.float64 else U32) <= 1.0
