@@ -63,56 +63,35 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-// Row maxima of |x(r, p)| as bit patterns, rows contiguous (a column-major
-// A). A block covers 32 rows x 256 of p, reads along r with all of a thread's
-// 32 loads issued before the first maximum, reduces in registers / shared
-// memory and posts one atomicMax per row (maxbits must start at zero). At
-// 8192^2 this reads at 4.8 TB/s (108 us), against 3.8 for the run layout of
-// the other prep kernels (133 us); with p contiguous the run layout is the
-// faster one (132 us, against 230 for this kernel's lanes-along-p branch).
-__global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restrict__ x, int64_t sr, int64_t sp,
-                                                         int64_t R, int64_t K, bool r_contig,
-                                                         unsigned long long* __restrict__ maxbits) {
+// Row maxima of |x(r, p)| as bit patterns, rows contiguous (sr == 1, a
+// column-major A). A block covers 32 rows x 256 of p: lanes along r, the 8
+// warps striding over p, each thread's 32 loads issued before the first
+// maximum; the warps' maxima meet in shared memory and one atomicMax per row
+// posts them (maxbits must start at zero). At 8192^2 this reads at 4.8 TB/s
+// (108 us), against 3.8 for the run layout of the other prep kernels (133
+// us); with p contiguous the run layout is the faster one (132 us, against
+// 230 for a warp per row with lanes along p in this block shape).
+__global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restrict__ x, int64_t sp, int64_t R,
+                                                         int64_t K, unsigned long long* __restrict__ maxbits) {
   __shared__ unsigned long long red[8][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 256;
-  if (r_contig) {
-    // lanes along r, ty strides over p
-    const int64_t r = r0 + tx;
-    unsigned long long mx = 0;
-    if (r < R)
-      for (int j = 0; j < 32; ++j) {
-        const int64_t pp = p0 + ty + 8 * j;
-        if (pp < K) mx = max(mx, abs_bits(x[r * sr + pp * sp]));
-      }
-    red[ty][tx] = mx;
-    __syncthreads();
-    if (ty == 0 && r < R) {
-      for (int i = 1; i < 8; ++i) mx = max(mx, red[i][tx]);
-      if (mx) atomicMax(&maxbits[r], mx);
-    }
-  } else {
-    // one warp per row, lanes along p
-    double v[4][8];
+  const int64_t r = (int64_t)blockIdx.y * 32 + tx, p0 = (int64_t)blockIdx.x * 256;
+  unsigned long long mx = 0;
+  if (r < R) {
+    double v[32];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int64_t r = r0 + ty + 8 * i;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int64_t pp = p0 + tx + 32 * j;
-        v[i][j] = (r < R && pp < K) ? x[r * sr + pp * sp] : 0.0;
-      }
+    for (int j = 0; j < 32; ++j) {
+      const int64_t pp = p0 + ty + 8 * j;
+      v[j] = pp < K ? x[r + pp * sp] : 0.0;
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int64_t r = r0 + ty + 8 * i;
-      unsigned long long mx = 0;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) mx = max(mx, abs_bits(v[i][j]));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (tx == 0 && mx && r < R) atomicMax(&maxbits[r], mx);
-    }
+    for (int j = 0; j < 32; ++j) mx = max(mx, abs_bits(v[j]));
+  }
+  red[ty][tx] = mx;
+  __syncthreads();
+  if (ty == 0 && r < R) {
+    for (int i = 1; i < 8; ++i) mx = max(mx, red[i][tx]);
+    if (mx) atomicMax(&maxbits[r], mx);
   }
 }
 
@@ -606,7 +585,7 @@ int ozaki_operand_exponents(const double* x, int64_t sr, int64_t sp, int64_t R, 
     for (int64_t rb = 0; rb < R; rb += (int64_t)65535 * 32, ++launches) {
       const int64_t rn = std::min<int64_t>(R - rb, (int64_t)65535 * 32);
       row_absmax_kernel<<<dim3((unsigned)ceil_div(K, 256), (unsigned)ceil_div(rn, 32)), dim3(32, 8), 0, s>>>(
-          x + rb * sr, sr, sp, rn, K, true, maxbits + rb);
+          x + rb, sp, rn, K, maxbits + rb);
     }
   } else {
     const int lg = planes::run_lanes_log2(K, 8, false, planes::kRowsContigLg);
