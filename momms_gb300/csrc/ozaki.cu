@@ -67,10 +67,10 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
 // column-major A). A block covers 32 rows x 256 of p: lanes along r, the 8
 // warps striding over p, each thread's 32 loads issued before the first
 // maximum; the warps' maxima meet in shared memory and one atomicMax per row
-// posts them (maxbits must start at zero). At 8192^2 this reads at 4.8 TB/s
-// (108 us), against 3.8 for the run layout of the other prep kernels (133
-// us); with p contiguous the run layout is the faster one (132 us, against
-// 230 for a warp per row with lanes along p in this block shape).
+// posts them (maxbits must start at zero). At 8192^2 this reads at 5.0 TB/s
+// (104-108 us), against 4.0 for the run layout of the other prep kernels
+// (133 us); with p contiguous the run layout is the faster one (132 us,
+// against 230 for a warp per row with lanes along p in this block shape).
 __global__ void __launch_bounds__(256) row_absmax_kernel(const double* __restrict__ x, int64_t sp, int64_t R,
                                                          int64_t K, unsigned long long* __restrict__ maxbits) {
   __shared__ unsigned long long red[8][33];
