@@ -270,3 +270,19 @@ def test_operand_passes_layout_independent(gpu, prec, shape):
         assert np.array_equal(C, ref), (a_kind, b_kind)
     exact, mag = ou.dd_gemm(A.astype(np.float64), B.astype(np.float64), C0.astype(np.float64), alpha=0.5, beta=-1.0)
     assert ou.bound_ratio(ref, exact, mag, k, U64 if dt == np.float64 else U32) <= 1.0
+
+
+def test_ozaki_rows_past_one_launch_of_row_maxima(gpu):
+    """Row maxima of a column-major A run in launches of 65535 x 32 rows: a
+    2.2 M-row A (row scales spread over 2^-30..2^30, so a wrong row exponent
+    shows) is inside the FP64-level bound on every entry, rows past the first
+    launch included."""
+    rng = np.random.default_rng(22)
+    m, n, k = 2_200_000, 8, 8
+    A = np.asfortranarray(rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-30, 31, m))[:, None])
+    B = np.asfortranarray(rng.uniform(-1, 1, (k, n)))
+    C0 = np.asfortranarray(rng.uniform(-1, 1, (m, n)))
+    C = gu.gemm_device(gpu, A, B, C0, 1.0, 0.5, precision=mg.PREC_OZAKI)
+    ref, mag = ou.dd_gemm(A, B, C0, alpha=1.0, beta=0.5)
+    assert ou.bound_ratio(C, ref, mag, k, U64) <= 1.0
+    assert ou.bound_ratio(C[65535 * 32:], ref[65535 * 32:], mag[65535 * 32:], k, U64) <= 1.0
