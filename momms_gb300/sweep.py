@@ -112,6 +112,7 @@ def run_one(lib, torch, dtype, prec, m, n, k, phi=None, reps=3, warmup=1, err=Fa
            "tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12}
     if prec == mg.PREC_OZAKI:
         out["slices"] = info.slices
+        out["pairs"] = info.pairs
         out["bound_rel_err"] = info.bound_rel_err
     if phi is not None:
         out["phi"] = phi
@@ -124,12 +125,18 @@ def run_one(lib, torch, dtype, prec, m, n, k, phi=None, reps=3, warmup=1, err=Fa
 
 
 def roofline(o, pk):
+    """Adds achieved GB/s (A, B and C once each) and, where the work per
+    product is known, the bound min(peak, intensity x HBM) in FP64/f32
+    TFLOP/s of the call and the fraction reached. Emulated FP64 runs
+    `pairs` fp16 slice products per output product, so its peak is the fp16
+    rate divided by the pair count."""
     es = 8 if o["dtype"] == "f64" else 4
     m, n, k = o["m"], o["n"], o["k"]
     bytes_ = es * (m * k + k * n + m * n)  # beta = 0: C written once
     flops = 2.0 * m * n * k
+    ozaki_peak = pk["f16_tflops"] / o["pairs"] if o.get("pairs") else None
     peak = {"plain": pk["f64_tflops"] if o["dtype"] == "f64" else pk["f32_tflops"],
-            "ozaki": None, "tf32": pk["tf32_tflops"] / 3}[o["prec"]]
+            "ozaki": ozaki_peak, "tf32": pk["tf32_tflops"] / 3}[o["prec"]]
     o["gbs"] = bytes_ / (o["ms"] * 1e-3) / 1e9
     if peak is not None:
         bound = min(peak, flops / bytes_ * pk["hbm_gbs"] / 1e3)

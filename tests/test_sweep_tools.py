@@ -46,8 +46,20 @@ def test_roofline_bound():
                         "tflops": 10.7}, pk)
     flops, bytes_ = 2.0 * 8192 * 8192 * 8, 4 * (8192 * 8 * 2 + 8192 * 8192)
     assert abs(o["bound_tflops"] - flops / bytes_ * 6760.6 / 1e3) < 1e-9 and o["bound_tflops"] < 78.0
+    # emulated FP64 without a pair count: no bound; with 28 slice products per
+    # output product the peak is the fp16 rate / 28 (67.6 TFLOP/s), below the
+    # rank-64 HBM limit (15.8 flop/B x 6.76 TB/s = 107 TFLOP/s)
     assert "bound_tflops" not in sweep.roofline({"dtype": "f64", "prec": "ozaki", "m": 64, "n": 64, "k": 64,
                                                  "ms": 1.0, "tflops": 1.0}, pk)
+    o = sweep.roofline({"dtype": "f64", "prec": "ozaki", "m": 8192, "n": 8192, "k": 64, "ms": 1.17,
+                        "tflops": 7.35, "slices": 7, "pairs": 28}, pk)
+    assert abs(o["bound_tflops"] - 1891.8 / 28) < 1e-9
+    assert abs(o["frac_of_bound"] - 7.35 / (1891.8 / 28)) < 1e-12
+    # rank 8: the HBM limit (2 flop/B x 6.76 TB/s) is the bound
+    o = sweep.roofline({"dtype": "f64", "prec": "ozaki", "m": 8192, "n": 8192, "k": 8, "ms": 0.5,
+                        "tflops": 2.0, "slices": 7, "pairs": 28}, pk)
+    flops, bytes_ = 2.0 * 8192 * 8192 * 8, 8 * (8192 * 8 * 2 + 8192 * 8192)
+    assert abs(o["bound_tflops"] - flops / bytes_ * 6760.6 / 1e3) < 1e-9
 
 
 def test_slice_sweep_table_format():
