@@ -8,13 +8,14 @@
 // Work is cut into runs: RUN consecutive elements of one row, RUN * sizeof
 // of the plane type = 16 bytes, so that a run's values of one plane leave in
 // one vector store. The warp layout follows the source's contiguous index:
-//   * rows contiguous (a column-major A): a warp takes 8 consecutive rows x
-//     4 consecutive runs (lane = 8 * run + row), so each of a thread's RUN
-//     loads reads four 64-byte pieces (8 rows of 4 columns) and each plane
-//     store writes 64 contiguous bytes (4 runs) of each of 8 rows: whole
-//     32-byte sectors. (With a warp on 32 rows of one run, every store was 32
-//     separate 16-byte pieces, one L2 write request each, and the digit pass
-//     was store-throttled.);
+//   * rows contiguous (a column-major A): a warp takes 4 consecutive rows x
+//     8 consecutive runs (lane = 4 * run + row), so each of a thread's RUN
+//     loads reads eight 32-byte pieces (4 rows of 8 columns) and each plane
+//     store writes 128 contiguous bytes (8 runs) of each of 4 rows: whole
+//     lines. (With a warp on 32 rows of one run, every store was 32 separate
+//     16-byte pieces, one L2 write request each, and the digit pass was
+//     store-throttled; the read-only and single-plane passes use 8 rows x 4
+//     runs, see kRowsContigLg.);
 //   * otherwise (p contiguous, or general strides): the lanes take 32
 //     consecutive runs of one row, read with 16-byte vector loads where the
 //     row is aligned, and each plane store is one contiguous 512-byte warp
@@ -66,11 +67,12 @@ inline int run_lanes_log2(int64_t K, int run, bool r_contig, int rows_contig_lg)
   while (lg < 5 && ((int64_t)1 << lg) < runs) ++lg;
   return r_contig ? std::min(lg, rows_contig_lg) : lg;
 }
-// Rows-contiguous lanes per row (log2) of the prep kernels: 4 runs of a row
-// per warp, 8 rows (measured at 8192^2 digits: 0.28 ms, against 0.35 ms for
-// 16 rows x 2 runs and 1.02 ms for 32 rows x 1 run, whose 16-byte row pieces
-// cost one L2 write request each).
-constexpr int kRowsContigLg = 2;
+// Rows-contiguous lanes per row (log2) of the prep kernels. Digits of an
+// 8192^2 A (7 planes per run): 8 runs x 4 rows 0.243 ms, 4 runs x 8 rows
+// 0.277 ms, 2 x 16 0.352 ms, 1 x 32 1.02 ms (16-byte row pieces, one L2 write
+// request each). The magnitudes (one plane) and row maxima read alike at
+// every shape tried and keep 4 runs x 8 rows.
+constexpr int kRowsContigLg = 2, kRowsContigLgPlanes = 3;
 
 // Loads the run of row xr starting at p (p a multiple of RUN): RUN elements,
 // zeros past K. `vec`: p contiguous and the row 16-byte aligned, so the run
@@ -164,7 +166,7 @@ void launch_to_planes(const Tin* x, int64_t sr, int64_t sp, int64_t R, int64_t K
   }
   const bool r_contig = (sr == 1 && sp != 1);
   const bool vec = rows_vector_aligned(x, sr, sp);
-  const int lg = run_lanes_log2(K, RUN, r_contig, kRowsContigLg);
+  const int lg = run_lanes_log2(K, RUN, r_contig, kRowsContigLgPlanes);
   if (r_contig)
     to_planes_kernel<true, Tin, Op>
         <<<run_grid<true, RUN>(R, K, lg), THREADS, 0, s>>>(x, sr, sp, R, K, vec, lg, planes, ldp, plane_elems, op);
