@@ -1,6 +1,7 @@
-"""The reference arm of bench.py on the CPU: one JSON line with the keys a
-driver reads, and under torchrun a line from rank 0 only (the other ranks
-exit 0 without work)."""
+"""bench.py on the CPU: the reference arm's JSON line with the keys a driver
+reads, under torchrun a line from rank 0 only (the other ranks exit 0
+without work), and the replicas' timing plumbing (barrier, max over ranks)
+on two gloo ranks."""
 import json
 import os
 import subprocess
@@ -53,3 +54,37 @@ def test_reference_arm_under_torchrun_prints_once():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1
     _check_line(lines[0], 2)
+
+
+def _rank_worker(rank, world, port, results):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        bench.barrier(world)
+        # each rank's timed total differs; every rank must see the slowest
+        results[rank] = bench.max_over_ranks(1.5 * (rank + 1), world)
+        bench.barrier(world)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_timing_takes_the_slowest_rank():
+    """The replicas' timing plumbing of bench.py (barrier, max over ranks) on
+    two gloo ranks: both ranks get the larger of the two totals."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as mgr:
+        results = mgr.dict()
+        procs = [ctx.Process(target=_rank_worker, args=(r, 2, 29531, results)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(timeout=300)
+            assert p.exitcode == 0
+        assert dict(results) == {0: 3.0, 1: 3.0}
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(2.5, 1) == 2.5
