@@ -103,7 +103,6 @@ __global__ void __launch_bounds__(planes::THREADS)
                            int lg, unsigned long long* __restrict__ maxbits) {
   constexpr int RUN = 8;
   const planes::Chunk<false> c(lg);
-  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * planes::PITER;
   // the row loop's trip count is the same for every thread of the block, so
   // every lane reaches the shuffles
   for (int64_t rb = (int64_t)blockIdx.y * c.rows; rb < R; rb += (int64_t)gridDim.y * c.rows) {
@@ -113,7 +112,7 @@ __global__ void __launch_bounds__(planes::THREADS)
       const double* xr = x + r * sr;
 #pragma unroll 1
       for (int it = 0; it < planes::PITER; ++it) {
-        const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+        const int64_t p = planes::run_col(blockIdx.x, c, it, RUN);
         if (p >= K) break;
         double v[RUN];
         planes::load_run<false, RUN>(xr, sp, p, K, vec, v);
@@ -917,7 +916,6 @@ __global__ void __launch_bounds__(planes::THREADS)
                      unsigned long long* __restrict__ sums, bool indicator) {
   constexpr int RUN = 8;
   const planes::Chunk<R_CONTIG> c(lg);
-  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * planes::PITER;
   // the row loop's trip count is the same for every thread of the block
   // (rows past R only skip their work), so every lane reaches the shuffles
   for (int64_t rb = (int64_t)blockIdx.y * c.rows; rb < R; rb += (int64_t)gridDim.y * c.rows) {
@@ -929,7 +927,7 @@ __global__ void __launch_bounds__(planes::THREADS)
       uint16_t* outr = plane + r * ldp;
 #pragma unroll 1
       for (int it = 0; it < planes::PITER; ++it) {
-        const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+        const int64_t p = planes::run_col(blockIdx.x, c, it, RUN);
         if (p >= K) break;
         double v[RUN];
         planes::load_run<R_CONTIG, RUN>(xr, sp, p, K, vec, v);

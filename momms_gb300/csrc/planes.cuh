@@ -42,20 +42,32 @@ constexpr int THREADS = 256, PITER = 4;
 // rows, run ru of the runs taken across the chunk per iteration. A warp
 // holds 32 >> lg rows of 2^lg runs each; rows contiguous: consecutive lanes
 // take consecutive rows (lane = run * rows_per_warp + row), otherwise
-// consecutive runs of a row.
-template <bool R_CONTIG>
-struct Chunk {
+// consecutive runs of a row. Host-callable, so that the index arithmetic is
+// checked on the CPU.
+struct RunPlace {
   int rows, runs, rl, ru;
-  __device__ __forceinline__ explicit Chunk(int lg) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (R_CONTIG) {
-      const int rpw = 32 >> lg;
-      rows = (THREADS / 32) * rpw, runs = 1 << lg, rl = warp * rpw + (lane & (rpw - 1)), ru = lane >> (5 - lg);
-    } else {
-      rows = (THREADS / 32) << (5 - lg), runs = 1 << lg;
-      rl = (warp << (5 - lg)) + (lane >> lg), ru = lane & (runs - 1);
-    }
+};
+template <bool R_CONTIG>
+__host__ __device__ __forceinline__ RunPlace run_place(int tid, int lg) {
+  const int lane = tid & 31, warp = tid >> 5;
+  RunPlace c;
+  if (R_CONTIG) {
+    const int rpw = 32 >> lg;
+    c.rows = (THREADS / 32) * rpw, c.runs = 1 << lg, c.rl = warp * rpw + (lane & (rpw - 1)), c.ru = lane >> (5 - lg);
+  } else {
+    c.rows = (THREADS / 32) << (5 - lg), c.runs = 1 << lg;
+    c.rl = (warp << (5 - lg)) + (lane >> lg), c.ru = lane & (c.runs - 1);
   }
+  return c;
+}
+// First column of the thread's run `it` in block column bx (runs of `run`
+// elements; a block covers runs * run * PITER columns).
+__host__ __device__ __forceinline__ int64_t run_col(int64_t bx, const RunPlace& c, int it, int run) {
+  return (bx * c.runs * PITER + c.ru + (int64_t)c.runs * it) * run;
+}
+template <bool R_CONTIG>
+struct Chunk : RunPlace {
+  __device__ __forceinline__ explicit Chunk(int lg) : RunPlace(run_place<R_CONTIG>((int)threadIdx.x, lg)) {}
 };
 
 // Lanes per row (log2) for rows of K elements in runs of RUN: rows not
@@ -110,7 +122,6 @@ __global__ void __launch_bounds__(THREADS)
   constexpr int RUN = 16 / sizeof(Tout), NP = Op::PLANES;
   static_assert(sizeof(Word) == 2 * sizeof(Tout), "a word is one pair's value");
   const Chunk<R_CONTIG> c(lg);
-  const int64_t pc = (int64_t)blockIdx.x * c.runs * RUN * PITER;
   // row chunks beyond the grid's y limit are taken in further passes
   for (int64_t r = (int64_t)blockIdx.y * c.rows + c.rl; r < R; r += (int64_t)gridDim.y * c.rows) {
     const auto ctx = op.row(r);
@@ -118,7 +129,7 @@ __global__ void __launch_bounds__(THREADS)
     Tout* outr = planes + r * ldp;
 #pragma unroll 1
     for (int it = 0; it < PITER; ++it) {
-      const int64_t p = pc + (int64_t)(c.ru + c.runs * it) * RUN;
+      const int64_t p = run_col(blockIdx.x, c, it, RUN);
       if (p >= K) break;
       Tin v[RUN];
       load_run<R_CONTIG, RUN>(xr, sp, p, K, vec, v);
