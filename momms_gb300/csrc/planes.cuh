@@ -14,15 +14,16 @@
 //     store writes 128 contiguous bytes (8 runs) of each of 4 rows: whole
 //     lines. (With a warp on 32 rows of one run, every store was 32 separate
 //     16-byte pieces, one L2 write request each, and the digit pass was
-//     store-throttled; the read-only and single-plane passes use 8 rows x 4
-//     runs, see kRowsContigLg.);
+//     store-throttled. The read-only and single-plane passes use 8 rows x 4
+//     runs, see kRowsContigLg.)
 //   * otherwise (p contiguous, or general strides): the lanes take 32
 //     consecutive runs of one row, read with 16-byte vector loads where the
 //     row is aligned, and each plane store is one contiguous 512-byte warp
 //     access. Rows shorter than 32 runs share a warp: 2^lg lanes per row,
 //     2^lg the smallest power of two covering the row's runs.
 // Nothing goes through shared memory and nothing waits at a barrier. A
-// thread converts PITER runs of its row (PITER warp-widths apart along p).
+// thread converts PITER runs of its row, each `runs` runs after the last
+// (the runs of the warp's other lanes on that row lie in between).
 // (Loading the next run while converting the current one took more
 // registers than it hid latency: 0.277 -> 0.284 ms for the digits of A,
 // 0.14 -> 0.17 ms for the magnitudes, at 8192^2.)
