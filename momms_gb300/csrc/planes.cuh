@@ -152,8 +152,10 @@ __global__ void __launch_bounds__(THREADS)
   }
 }
 
-// Grid of a run kernel over an R x K view (lg: run_lanes_log2, used when
-// rows are not contiguous).
+// Grid of a run kernel over an R x K view, lg from run_lanes_log2: a block
+// holds 256 >> lg rows of 2^lg runs in either layout (the layouts differ in
+// which lanes take which place, run_place). Rows past 65535 blocks are taken
+// by the kernels' row loops.
 template <bool R_CONTIG, int RUN>
 inline dim3 run_grid(int64_t R, int64_t K, int lg) {
   const int64_t rows = (int64_t)(THREADS / 32) << (5 - lg);
