@@ -1,7 +1,8 @@
 """bench.py on the CPU: the reference arm's JSON line with the keys a driver
 reads, under torchrun a line from rank 0 only (the other ranks exit 0
-without work), and the replicas' timing plumbing (barrier, max over ranks)
-on two gloo ranks."""
+without work), the replicas' timing plumbing (barrier, max over ranks) on
+two gloo ranks, and the helpers behind the clocks, roofline.traffic and
+accuracy keys."""
 import json
 import os
 import subprocess
@@ -88,3 +89,75 @@ def test_replica_timing_takes_the_slowest_rank():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.max_over_ranks(2.5, 1) == 2.5
+
+
+def _bench():
+    sys.path.insert(0, ROOT)
+    import bench
+    return bench
+
+
+class _DoneProc:
+    """Stands in for the nvidia-smi process once its lines are in."""
+
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_sampler_keeps_the_timed_window():
+    """The clocks key: median SM clock of the samples inside the timed window
+    (one period of slack at the end), the max clock, and every throttle
+    reason seen active there; samples outside the window do not count."""
+    bench = _bench()
+    s = bench.ClockSampler(0)
+    s.proc = _DoneProc()
+    na, act = "Not Active", "Active"
+
+    def ln(sm, reasons):
+        return f"0, {sm}, 2070, 1100.5, 0x0, {reasons[0]}, {reasons[1]}, {reasons[2]}, {reasons[3]}"
+    s.lines = [(0.50, ln(2070, (na, na, na, na))),           # before the window
+               (1.00, ln(1800, (na, na, na, act))),
+               (1.20, ln(1700, (na, na, na, act))),
+               (1.40, ln(1750, (na, na, na, na))),
+               (1.54, ln(1650, (na, na, na, na))),           # inside the slack after t1
+               (2.00, ln(1000, (act, na, na, na)))]          # after the window
+    out = s.stop(1.0, 1.5)
+    assert out["samples"] == 4 and out["sm_mhz"] == 1725.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"]
+    # a window shorter than the period takes the first sample after it starts
+    s2 = bench.ClockSampler(0)
+    s2.proc = _DoneProc()
+    s2.lines = [(0.9, ln(2000, (na,) * 4)), (1.3, ln(1900, (na, na, act, na)))]
+    out = s2.stop(1.0, 1.01)
+    assert out["samples"] == 1 and out["sm_mhz"] == 1900.0 and out["reasons"] == ["sw_thermal_slowdown"]
+    # no nvidia-smi: the key says so
+    assert bench.ClockSampler(0).stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_profile_traffic_reads_the_committed_summaries():
+    """roofline.traffic comes from the ncu summaries under profiles/."""
+    bench = _bench()
+    for tag in ("slice_gemm_ozaki_8192", "dgemm_dmma_8192"):
+        t = bench.profile_traffic(tag)
+        assert t is not None and 1e9 < t < 1e12, tag
+    assert bench.profile_traffic("no_such_profile") is None
+
+
+def test_sampled_error_is_exact_and_catches_a_wrong_entry():
+    """The accuracy key: zero on data whose products and sums are exact in
+    FP64, and the relative size of a planted error in one sampled entry."""
+    import numpy as np
+    bench = _bench()
+    rng = np.random.default_rng(3)
+    A = np.asfortranarray(rng.integers(-8, 9, (64, 40)).astype(np.float64))
+    B = np.asfortranarray(rng.integers(-8, 9, (40, 48)).astype(np.float64))
+    C0 = np.asfortranarray(rng.integers(-8, 9, (64, 48)).astype(np.float64))
+    C = C0 + A @ B
+    assert bench.sampled_error(A, B, C0, C, samples=4000) == 0.0
+    bad = C.copy()
+    bad[:, :] += 1e-6 * (np.abs(A) @ np.abs(B) + np.abs(C0))
+    err = bench.sampled_error(A, B, C0, bad, samples=64)
+    assert 0.5e-6 < err < 2e-6
