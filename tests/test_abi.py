@@ -151,3 +151,39 @@ def test_fault_injection_counters_without_a_gpu(lib):
     assert lib.momms_fault_inject(9, 1) == mg.ERR_INVALID_ARG
     assert lib.momms_fault_inject(mg.FAULT_CUDA, -1) == mg.ERR_INVALID_ARG
     assert lib.momms_fault_pending(9) == -1
+
+
+def test_no_cpu_fallback(lib, tmp_path):
+    """Without a GPU every compute mode returns MOMMS_ERR_NO_DEVICE and leaves
+    C untouched (nothing is computed on the host), and a missing library is
+    an ImportError, not a silent fallback."""
+    import numpy as np
+    if _torch_cuda():
+        pytest.skip("a GPU is present")
+    A = np.asfortranarray(np.ones((4, 3)))
+    B = np.asfortranarray(np.ones((3, 5)))
+    C = np.asfortranarray(np.full((4, 5), 7.0))
+
+    def trip(x):
+        return (x.ctypes.data, x.strides[0] // x.itemsize, x.strides[1] // x.itemsize)
+
+    for dt, prec in ((mg.DTYPE_F64, mg.PREC_PLAIN), (mg.DTYPE_F64, mg.PREC_OZAKI)):
+        d = gu.make_desc(dt, 4, 5, 3, 1.0, 1.0, trip(A), trip(B), trip(C), precision=prec, mem=mg.MEM_HOST)
+        assert lib.momms_gemm(ctypes.byref(d), None) == mg.ERR_NO_DEVICE
+        assert np.all(C == 7.0)
+    A32, B32, C32 = (np.asfortranarray(x.astype(np.float32)) for x in (A, B, C))
+    for prec in (mg.PREC_PLAIN, mg.PREC_SPLIT_TF32):
+        d = gu.make_desc(mg.DTYPE_F32, 4, 5, 3, 1.0, 1.0, trip(A32), trip(B32), trip(C32), precision=prec,
+                         mem=mg.MEM_HOST)
+        assert lib.momms_gemm(ctypes.byref(d), None) == mg.ERR_NO_DEVICE
+        assert np.all(C32 == 7.0)
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        mg.load_library(path=str(tmp_path / "libmomms_gpu.so"))
+
+
+def _torch_cuda():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except ImportError:
+        return False
