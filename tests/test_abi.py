@@ -187,3 +187,10 @@ def _torch_cuda():
         return torch.cuda.is_available()
     except ImportError:
         return False
+
+
+def test_integration_notes_bind_every_function():
+    """INTEGRATION.md shows the binding of every function include/*.h declares."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in declared_functions() if not re.search(r"\b%s\b" % n, text)]
+    assert not missing, missing
