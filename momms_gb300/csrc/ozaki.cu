@@ -37,13 +37,18 @@
 
 #include "internal.h"
 #include "exact_round.cuh"
+#include "ozaki_elem.cuh"
 #include "planes.cuh"
 #include "slicegemm.cuh"
 
 namespace momms {
 namespace {
 
-constexpr int kDigitBits = 8;
+constexpr int kDigitBits = elem::kDigitBits;
+using elem::abs_bits;
+using elem::exponent_of_max;
+using elem::magnitude;
+using elem::offset_digits;
 // k per launch (kOzakiMaxK): the largest product of two digits is 2^16, so a
 // single pair's int32 sum stays below 2^31 for up to 511 k-blocks of 64
 constexpr int64_t kMaxK = kOzakiMaxK;
@@ -55,13 +60,6 @@ constexpr double kChunkBound = 16777216.0;
 
 // Everything in the pre-pass runs on integer bit patterns: GB300's FP64 pipe
 // is about 1 TFLOP/s, so FP64 arithmetic per element would dominate.
-
-// |v| as an unsigned bit pattern: for non-negative doubles the unsigned order
-// of the patterns is the order of the values; infinities and NaNs sort above
-// every finite value.
-__device__ __forceinline__ unsigned long long abs_bits(double v) {
-  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-}
 
 // Row maxima of |x(r, p)| as bit patterns, rows contiguous (sr == 1, a
 // column-major A). A block covers 32 rows x 256 of p: lanes along r, the 8
@@ -125,50 +123,10 @@ __global__ void __launch_bounds__(planes::THREADS)
   }
 }
 
-// Exponent e with max |x| < 2^e (the frexp exponent of the maximum); 0 for an
-// all-zero row; INT32_MAX for a row holding a NaN or an infinity.
-// Exponent e of a row whose largest |v| has bit pattern b: |v| < 2^e.
-__device__ __forceinline__ int exponent_of_max(unsigned long long b) {
-  if (b >= 0x7ff0000000000000ull) return INT32_MAX;
-  if (b == 0) return 0;
-  if ((b >> 52) != 0) return (int)(b >> 52) - 1022;  // [2^(be-1023), 2^(be-1022))
-  return (63 - __clzll((long long)b)) - 1073;         // subnormal
-}
-
 __global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int64_t count, int* __restrict__ exps) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   exps[i] = exponent_of_max(maxbits[i]);
-}
-
-// Signed digits of v * 2^-e at kDigitBits bits each, nearest rounding at the
-// last digit: X = round(|v| * 2^(bits*NS - e)) as an integer, written as
-//   X = sum_{pos < NS-1} d_pos 2^(bits*pos) + top 2^(bits*(NS-1))
-// with centred lower digits d_pos in [-2^(bits-1), 2^(bits-1)) and the top
-// digit in [0, 2^bits]. That representation is unique, and all its digits come
-// at once from Y = X + H, H = 2^(bits-1) * sum_{pos < NS-1} 2^(bits*pos):
-// Y's plain base-2^bits digits are u_pos = d_pos + 2^(bits-1), and its bits
-// above position bits*(NS-1) are the top digit. Zero, and every element of a
-// row holding a NaN or an infinity (e == INT32_MAX), get X = 0: all digits 0.
-// U is uint64 (bits*NS <= 62) or __int128.
-template <int NS, typename U>
-__device__ __forceinline__ U offset_digits(double v, int e) {
-  constexpr int bits = kDigitBits, half = 1 << (bits - 1);
-  U H = 0;
-#pragma unroll
-  for (int pos = 0; pos < NS - 1; ++pos) H |= (U)half << (bits * pos);
-  const unsigned long long ab = abs_bits(v);
-  const unsigned long long frac = ab & ((1ull << 52) - 1);
-  const int be = (int)(ab >> 52);
-  const unsigned long long M = be ? (frac | (1ull << 52)) : frac;
-  const int E = be ? be - 1075 : -1074;  // |v| = M * 2^E
-  const int sh = E - e + bits * NS;
-  U X;
-  if (e == INT32_MAX) X = 0;
-  else if (sh >= 0) X = (U)M << sh;
-  else if (sh > -64) X = (U)((M >> (-sh)) + ((M >> (-sh - 1)) & 1ull));
-  else X = 0;
-  return X + H;
 }
 
 // Digit planes of an operand for NS slices: plane t holds digit position
@@ -856,49 +814,6 @@ void bound_work_carve(void* base, int64_t m, int64_t n, int64_t k, BoundWork* w)
   w->sum_a = reinterpret_cast<unsigned long long*>(p);
   w->sum_b = w->sum_a + m;
   w->out = reinterpret_cast<unsigned*>(w->sum_b + n);
-}
-
-// |v| 2^-e for the bound: as bf16 rounded toward zero (0 below bf16's normal
-// range: the lower bound only loses that term), and as ceil(|v| 2^(40 - e)),
-// an upward-rounded fixed-point term of the row sum. Integer arithmetic on
-// the bit pattern only. Rows holding a NaN or an infinity (e == INT32_MAX)
-// give 0: their results are NaN and need no bound. With `indicator`, *bf is
-// 1.0 for every element that is nonzero (in a finite row), else 0.
-__device__ __forceinline__ void magnitude(double v, int e, bool indicator, uint16_t* bf, unsigned long long* fix) {
-  *bf = 0;
-  *fix = 0;
-  const unsigned long long ab = abs_bits(v);
-  if (ab == 0 || e == INT32_MAX || ab >= 0x7ff0000000000000ull) return;
-  if (indicator) {
-    *bf = 0x3f80;  // 1.0
-    return;
-  }
-  const int be = (int)(ab >> 52);
-  if (be != 0 && be - 1023 - e <= -1) {
-    // normal v below 2^e (every element of a row but subnormals):
-    // |v| 2^-e in [2^X, 2^(X+1)) with X = be - 1023 - e. The bf16's 7
-    // fraction bits are the top of v's fraction, and |v| 2^(40-e) =
-    // M 2^-(12-X) is a right shift by at least 13: the general steps below,
-    // with the shift counts known.
-    const int X = be - 1023 - e;
-    if (X + 127 >= 1) *bf = (uint16_t)(((unsigned)(X + 127) << 7) | ((unsigned)(ab >> 45) & 0x7fu));
-    const int r = 12 - X;
-    const unsigned long long M = (ab & ((1ull << 52) - 1)) | (1ull << 52);
-    *fix = r < 64 ? (M >> r) + ((M << (64 - r)) != 0 ? 1ull : 0ull) : 1ull;
-    return;
-  }
-  const unsigned long long M = be ? ((ab & ((1ull << 52) - 1)) | (1ull << 52)) : ab;
-  const int E = be ? be - 1075 : -1074;           // |v| = M 2^E
-  const int nb = 64 - __clzll((long long)M);      // significant bits of M
-  const int X = E - e + nb - 1;                   // |v| 2^-e in [2^X, 2^(X+1)), X <= -1
-  if (X + 127 >= 1) {
-    const unsigned top = (unsigned)(nb >= 8 ? (M >> (nb - 8)) : (M << (8 - nb)));  // leading 8 bits
-    *bf = (uint16_t)(((unsigned)(X + 127) << 7) | (top & 0x7fu));
-  }
-  const int sh = E - e + 40;  // |v| 2^(40-e) = M 2^sh < 2^40
-  if (sh >= 0) *fix = M << sh;
-  else if (sh > -64) *fix = (M >> (-sh)) + ((M & ((1ull << (-sh)) - 1)) ? 1ull : 0ull);
-  else *fix = 1ull;
 }
 
 // Magnitude plane and row sums of an R x K view (element (r, p) at
